@@ -1,0 +1,165 @@
+/*
+ * r2p.h -- C ABI of the GB300 raw-pixel -> PNG encoder (libr2p.so).
+ *
+ * Plain C types only: pointers, sizes, ints.  Device pointers are CUDA
+ * device addresses on the current device; `stream` arguments are cudaStream_t
+ * handles passed as void* (NULL = the legacy default stream).  Every entry
+ * point returns an R2P_* status and never exits the process; the reference
+ * printed and called exit(1) on every CUDA error (src/gpu_filter.cu:25-33).
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the HeC-KriS/RAW2PNG-ConversionThruGPU project root).
+ */
+#ifndef R2P_H
+#define R2P_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define R2P_OK        0
+#define R2P_EINVAL    1   /* bad argument or unsupported geometry */
+#define R2P_ENOMEM    2   /* device or pinned allocation failed */
+#define R2P_EBUDGET   3   /* request exceeds the engine's HBM budget */
+#define R2P_ECUDA     4   /* CUDA runtime error (message via r2p_last_error) */
+#define R2P_ETIMEOUT  5   /* a bounded wait gave up */
+#define R2P_ENOSPC    6   /* caller's output buffer is too small */
+#define R2P_ECANCELED 7   /* request cancelled before it ran */
+#define R2P_ENOTFOUND 8   /* unknown ticket */
+
+/* ---- window modes ------------------------------------------------------ */
+/* R2P_WINDOW_NONE: samples are already in PNG byte order (16-bit big-endian,
+ *   as the TIFF/RAW loaders deliver them, src/image_loader.cpp:200-202).
+ * R2P_WINDOW_SWAP16: 16-bit little-endian samples, byte-swapped only.
+ * R2P_WINDOW_DICOM16: DICOM shift/mask/sign/rescale/window with output depth
+ *   equal to BitsAllocated (dicom_preprocess_kernel, src/gpu_filter.cu:71-162).
+ * R2P_WINDOW_BATCH8: 16-bit grayscale DICOM converted to 8 bits the way the
+ *   folder batch does it (src/batch_processor.cpp:397-409: Q15 linear map
+ *   when eligible, else the FP32 table). */
+#define R2P_WINDOW_NONE    0
+#define R2P_WINDOW_SWAP16  1
+#define R2P_WINDOW_DICOM16 2
+#define R2P_WINDOW_BATCH8  3
+
+/* Same layout as DicomPixelParams (include/dicom_params.h:6-21). */
+typedef struct r2p_dicom_params {
+    int   bits_allocated;
+    int   bits_stored;
+    int   high_bit;
+    int   pixel_rep;
+    int   apply_rescale;
+    float rescale_slope;
+    float rescale_intercept;
+    int   apply_window;
+    float window_center;
+    float window_width;
+} r2p_dicom_params;
+
+/* One image to encode.  level 0 = stored DEFLATE blocks; 1..9 = LZ77 with the
+ * fixed Huffman code in independent blocks (the zlib header's FLEVEL bits
+ * follow the level exactly as src/parallel_deflate.cpp:214-228 sets them).
+ * strip_height keeps the CLI's meaning for the strip-wise entry points; the
+ * whole-image entry points hold the image resident and ignore it. */
+typedef struct r2p_image {
+    uint32_t width;
+    uint32_t height;
+    int      channels;          /* 1 gray, 3 RGB, 4 RGBA */
+    int      bytes_per_sample;  /* input: 1 or 2 */
+    int      window_mode;       /* R2P_WINDOW_* */
+    r2p_dicom_params dicom;     /* used by DICOM16 / BATCH8 */
+    int      level;             /* 0..9 */
+    int      strip_height;
+    int      block_size;        /* 0 = automatic (size-class table), else filtered bytes per DEFLATE block */
+} r2p_image;
+
+/* ---- library ----------------------------------------------------------- */
+int         r2p_version(void);
+const char* r2p_status_string(int status);
+/* Message of the last R2P_ECUDA/R2P_EINVAL raised on the calling thread. */
+const char* r2p_last_error(void);
+
+/* ---- engine: device-owning encoder ------------------------------------- */
+typedef struct r2p_engine r2p_engine;
+
+/* Replaces the per-image GpuFilterContext/GpuDeflateContext/GpuAdler32Context/
+ * GpuPngAssembleContext set built in run_pipeline (src/pipeline.cpp:1579-1648)
+ * and its thread-local cache (:1527-1561).  hbm_budget = 0 means no limit. */
+int  r2p_engine_create(int device, size_t hbm_budget, r2p_engine** out);
+void r2p_engine_destroy(r2p_engine* eng);
+
+/* Upper bound of the PNG size for an image; 0 on invalid geometry. */
+size_t r2p_png_bound(const r2p_image* img);
+
+/* Encode one image from host memory to a PNG in host memory (blocking).
+ * Replaces encode_source_to_png(ImageSource&, out, cfg)
+ * (include/pipeline.h:110-112) minus the file write. */
+int r2p_encode_png(r2p_engine* eng, const r2p_image* img, const void* h_pixels,
+                   void* h_png, size_t png_cap, size_t* png_len);
+
+/* Device-resident form: pixels and PNG stay in HBM; the PNG size is written
+ * to *d_png_len (a device uint64) when the work on `stream` completes.
+ * Replaces the modern path's filter -> gpu_deflate -> gpu_adler32 ->
+ * gpu_png_assemble sequence (src/pipeline.cpp:581-830). */
+int r2p_encode_png_device(r2p_engine* eng, const r2p_image* img, const void* d_pixels,
+                          void* d_png, size_t png_cap, uint64_t* d_png_len, void* stream);
+
+/* Batched form: n images in one launch sequence (one kernel per stage over a
+ * device work list of row bands and DEFLATE blocks).  Replaces the folder
+ * batch's per-file encode pool (src/batch_processor.cpp:482-737). */
+int r2p_encode_batch_device(r2p_engine* eng, int n, const r2p_image* imgs,
+                            const void* const* d_pixels, void* const* d_pngs,
+                            const size_t* png_caps, uint64_t* d_png_lens, void* stream);
+
+/* Stage entry point: window + adaptive filter of a whole image into
+ * height*(row_bytes+1) filtered scanline bytes on the device.  d_prior (may
+ * be NULL = zeros) is the windowed row above row 0.  Replaces
+ * gpu_filter_process_from_device (include/gpu_filter.h:41-47). */
+int r2p_window_filter_device(r2p_engine* eng, const r2p_image* img, const void* d_pixels,
+                             const void* d_prior, void* d_filtered, void* stream);
+
+/* Stage entry point: zlib stream (header, DEFLATE blocks, Adler-32 trailer)
+ * of already-filtered bytes, on the device.  Replaces gpu_deflate_compress_strip
+ * + gpu_adler32 + zlib_header/trailer (include/gpu_deflate_backend.h:80-82,
+ * include/gpu_adler32.h:25-31, src/parallel_deflate.cpp:214-237). */
+int r2p_zlib_compress_device(r2p_engine* eng, const void* d_in, size_t len, int level,
+                             int block_size, void* d_out, size_t out_cap,
+                             uint64_t* d_out_len, void* stream);
+size_t r2p_zlib_bound(size_t len, int level, int block_size);
+
+/* ---- checksums (device data) ------------------------------------------- */
+/* Replace gpu_adler32_compute (include/gpu_adler32.h:25) and
+ * gpu_crc32_compute (include/gpu_crc32.h:29); results land in *d_result (a
+ * device uint32) on `stream`. */
+int r2p_adler32_device(r2p_engine* eng, const void* d_data, size_t len, uint32_t* d_result, void* stream);
+int r2p_crc32_device(r2p_engine* eng, const void* d_data, size_t len, uint32_t* d_result, void* stream);
+/* Host combine identities.  Replace gpu_crc32_combine (include/gpu_crc32.h:36)
+ * and zlib's adler32_combine as used by accum_adler (src/parallel_deflate.cpp:197-209). */
+uint32_t r2p_crc32_combine(uint32_t crc1, uint32_t crc2, uint64_t len2);
+uint32_t r2p_adler32_combine(uint32_t adler1, uint32_t adler2, uint64_t len2);
+
+/* ---- memory helpers (for callers without their own CUDA bindings) ------- */
+int  r2p_device_alloc(size_t bytes, void** d_ptr);
+int  r2p_device_free(void* d_ptr);
+int  r2p_host_alloc_pinned(size_t bytes, void** h_ptr);   /* gpu_filter_alloc_pinned, include/gpu_filter.h:29 */
+int  r2p_host_free_pinned(void* h_ptr);                   /* gpu_filter_free_pinned, include/gpu_filter.h:30 */
+int  r2p_memcpy(void* dst, const void* src, size_t bytes, void* stream); /* any direction, async on stream */
+int  r2p_memset_device(void* d_ptr, int value, size_t bytes, void* stream);
+int  r2p_stream_create(void** stream);
+int  r2p_stream_destroy(void* stream);
+int  r2p_stream_synchronize(void* stream);
+/* Events for device-side timing on a caller's stream. */
+int  r2p_event_create(void** ev);
+int  r2p_event_destroy(void* ev);
+int  r2p_event_record(void* ev, void* stream);
+int  r2p_event_elapsed_ms(void* ev_start, void* ev_end, float* ms);
+/* Kernels this library launched since the process started (all streams). */
+uint64_t r2p_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* R2P_H */

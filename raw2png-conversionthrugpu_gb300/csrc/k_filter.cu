@@ -1,0 +1,625 @@
+// k_filter.cu -- window/level + adaptive PNG filter, fused in one pass.
+//
+// Reference semantics:
+//   windowing, 16-bit out: dicom_preprocess_kernel   src/gpu_filter.cu:71-162
+//   windowing, 8-bit out : try_apply_linear_window   src/batch_processor.cpp:202-266
+//                          build/apply_dicom16_lut   src/batch_processor.cpp:100-185
+//                          dispatch                  src/batch_processor.cpp:397-409
+//   adaptive filter      : filter_select_kernel      src/gpu_filter.cu:183-309
+//
+// Design.  One CTA owns a band of consecutive rows of one image.  It windows
+// the raw rows into a ring of shared-memory row slots (16-byte coalesced loads
+// where the rows allow it) and keeps the last windowed row of a tile as the
+// "row above" of the next tile, so every raw byte is read once per band (plus
+// one row per band).  Each row is then scored for the five PNG filters by a
+// group of warps: four bytes per lane per step in SWAR arithmetic, costs summed
+// with a signed dp4a, warp shuffles for the reduction.  The winning filter is
+// recomputed and written straight to HBM with 4-byte stores realigned by a
+// funnel shift, so the filtered row never round-trips through shared memory.
+// Float arithmetic uses explicit IEEE intrinsics (no contraction), matching
+// the oracle's -ffp-contract=off restatement bit for bit.
+#include <cuda_runtime.h>
+
+#include "r2p_common.h"
+#include "r2p_device.h"
+#include "r2p_kernels.h"
+
+namespace r2p {
+
+// ---------------------------------------------------------------------------
+// Window formulas
+// ---------------------------------------------------------------------------
+
+// DICOM PS3.3 window with output depth = BitsAllocated (src/gpu_filter.cu:82-154),
+// applied to an already shifted-and-masked stored value (16-bit) or raw byte (8-bit).
+__device__ uint32_t a2_eval(uint32_t m, const r2p_dicom_params& p)
+{
+    const int out_max = (p.bits_allocated == 16) ? 65535 : 255;
+    float val;
+    if (p.bits_allocated == 16) {
+        if (p.pixel_rep == 1) {
+            int32_t sv;
+            if (p.bits_stored == 16) {
+                sv = (int32_t)(int16_t)(uint16_t)m;
+            } else {
+                const int half = 1 << (p.bits_stored - 1);
+                sv = (int32_t)m;
+                if (sv >= half) sv -= (1 << p.bits_stored);
+            }
+            val = (float)sv;
+        } else {
+            val = (float)m;
+        }
+    } else {
+        val = (p.pixel_rep == 1) ? (float)(int8_t)(uint8_t)m : (float)m;
+    }
+    if (p.apply_rescale) val = __fadd_rn(__fmul_rn(val, p.rescale_slope), p.rescale_intercept);
+    if (p.apply_window) {
+        const float wm1 = __fsub_rn(p.window_width, 1.0f);
+        const float cen = p.window_center;
+        if (wm1 <= 0.0f) {
+            val = (val >= cen) ? (float)out_max : 0.0f;
+        } else {
+            const float half = __fmul_rn(wm1, 0.5f);
+            const float lo = __fsub_rn(__fsub_rn(cen, half), 0.5f);
+            const float hi = __fsub_rn(__fadd_rn(cen, half), 0.5f);
+            if (val <= lo) {
+                val = 0.0f;
+            } else if (val > hi) {
+                val = (float)out_max;
+            } else {
+                const float t = __fadd_rn(__fsub_rn(val, cen), 0.5f);
+                const float q = __fdiv_rn(t, wm1);
+                val = __fmul_rn(__fadd_rn(q, 0.5f), (float)out_max);
+            }
+        }
+    }
+    const float hi = (float)out_max;
+    float v = (val < hi) ? val : hi;   // NaN -> hi, as fminf(hi, NaN)
+    v = (v > 0.0f) ? v : 0.0f;
+    return __float2uint_rz(v);
+}
+
+// Index into a window table: the stored value after shift and mask.
+__device__ __forceinline__ uint32_t win_index(uint32_t raw, int shift, uint32_t mask)
+{
+    return (raw >> shift) & mask;
+}
+
+// FP32 table entry of build_dicom16_lut (src/batch_processor.cpp:100-147).
+__device__ uint8_t lut8_eval(int i, int lut_size, const r2p_dicom_params& p)
+{
+    const int mask = lut_size - 1;
+    float norm_scale = 1.f, norm_offset = 0.f;
+    if (!p.apply_window) {
+        if (p.pixel_rep == 1) {
+            const float half = (float)(lut_size >> 1);
+            const float range = (float)lut_size;
+            norm_scale = __fdiv_rn(1.f, range);
+            norm_offset = __fdiv_rn(half, range);
+        } else {
+            norm_scale = __fdiv_rn(1.f, (float)(lut_size - 1));
+        }
+    }
+    float lo = 0.f, inv_range = 1.f;
+    if (p.apply_window) {
+        lo = __fsub_rn(p.window_center, __fmul_rn(p.window_width, 0.5f));
+        const float hi = __fadd_rn(p.window_center, __fmul_rn(p.window_width, 0.5f));
+        inv_range = (hi > lo) ? __fdiv_rn(1.f, __fsub_rn(hi, lo)) : 0.f;
+    }
+    float val;
+    if (p.pixel_rep == 1 && p.bits_stored < 16) {
+        const int sign_bit = lut_size >> 1;
+        int32_t s = i;
+        if (s & sign_bit) s |= ~mask;
+        val = (float)s;
+    } else if (p.pixel_rep == 1) {
+        val = (float)(int16_t)(uint16_t)(unsigned)i;
+    } else {
+        val = (float)(unsigned)i;
+    }
+    if (p.apply_rescale) val = __fadd_rn(__fmul_rn(val, p.rescale_slope), p.rescale_intercept);
+    const float norm = p.apply_window ? __fmul_rn(__fsub_rn(val, lo), inv_range)
+                                      : __fadd_rn(__fmul_rn(val, norm_scale), norm_offset);
+    const int v = __float2int_rz(__fadd_rn(__fmul_rn(norm, 255.f), 0.5f));
+    return (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+}
+
+// Q15 coefficients of try_apply_linear_window (src/batch_processor.cpp:202-251).
+// Returns false when the reference would decline and fall back to the table.
+__device__ bool q15_coeffs(const r2p_dicom_params& p, int32_t& A, int32_t& B)
+{
+    if (p.high_bit - p.bits_stored + 1 != 0) return false;
+    float A_f, B_f;
+    const float slope = p.apply_rescale ? p.rescale_slope : 1.f;
+    const float intercept = p.apply_rescale ? p.rescale_intercept : 0.f;
+    if (p.apply_window && p.window_width > 0.f) {
+        const float lo = __fsub_rn(p.window_center, __fmul_rn(p.window_width, 0.5f));
+        A_f = __fdiv_rn(__fmul_rn(slope, 255.f), p.window_width);
+        B_f = __fdiv_rn(__fmul_rn(__fsub_rn(intercept, lo), 255.f), p.window_width);
+    } else if (!p.apply_window) {
+        const float range = (float)(1u << p.bits_stored);
+        if (p.pixel_rep == 1) {
+            const float half = __fmul_rn(range, 0.5f);
+            A_f = __fdiv_rn(__fmul_rn(slope, 255.f), range);
+            B_f = __fdiv_rn(__fmul_rn(__fadd_rn(intercept, half), 255.f), range);
+        } else {
+            const float r1 = __fsub_rn(range, 1.f);
+            A_f = __fdiv_rn(__fmul_rn(slope, 255.f), r1);
+            B_f = __fdiv_rn(__fmul_rn(intercept, 255.f), r1);
+        }
+    } else {
+        return false;
+    }
+    const float A_q15 = __fmul_rn(A_f, 32768.f);
+    if (A_q15 < -32767.f || A_q15 > 32767.f) return false;
+    A = (int32_t)(int16_t)__float2int_rz(A_q15);
+    const float bs = __fmul_rn(B_f, 32768.f);
+    float bq;
+    if (A_f >= 0.f) bq = (A_q15 == (float)__float2int_rz(A_q15)) ? bs : __fadd_rn(bs, 0.5f);
+    else            bq = __fsub_rn(bs, 0.5f);
+    B = __float2int_rz(bq);
+    return true;
+}
+
+// Resolve each image's window request into a WinMode and build its table.
+// One CTA per image.
+__global__ void k_prepare_window(DevImage* imgs, int n)
+{
+    DevImage& d = imgs[blockIdx.x];
+    __shared__ int s_mode;
+    if (threadIdx.x == 0) {
+        int mode = W_COPY;
+        const r2p_dicom_params& p = d.dp;
+        d.lut_entries = 0;
+        d.lut_esize = 0;
+        d.lut_shift = 0;
+        d.lut_mask = 0;
+        if (d.req_mode == R2P_WINDOW_SWAP16) {
+            mode = (d.ib == 2) ? W_SWAP16 : W_COPY;
+        } else if (d.req_mode == R2P_WINDOW_DICOM16) {
+            int entries, shift = 0;
+            uint32_t mask;
+            if (d.ib == 2) {
+                const int bs = p.bits_stored;
+                const int sh = p.high_bit - bs + 1;
+                shift = sh > 0 ? sh : 0;
+                mask = (bs < 16) ? ((1u << bs) - 1u) : 0xFFFFu;
+                entries = (int)mask + 1;
+            } else {
+                mask = 0xFFu;
+                entries = 256;
+            }
+            d.lut_shift = shift;
+            d.lut_mask = mask;
+            d.lut_entries = entries;
+            d.lut_esize = d.ob;
+            mode = (entries * d.ob <= kMaxSmemLut) ? W_A2_LUT : W_A2_DIRECT;
+        } else if (d.req_mode == R2P_WINDOW_BATCH8) {
+            int32_t A, B;
+            if (q15_coeffs(p, A, B)) {
+                d.qa = A;
+                d.qb = B;
+                mode = W_Q15;
+            } else {
+                const int entries = 1 << p.bits_stored;
+                d.lut_entries = entries;
+                d.lut_esize = 1;
+                d.lut_shift = p.high_bit - p.bits_stored + 1;
+                d.lut_mask = (uint32_t)(entries - 1);
+                mode = W_LUT8;
+            }
+        }
+        d.mode = mode;
+        s_mode = mode;
+    }
+    __syncthreads();
+    const int mode = s_mode;
+    if (mode == W_A2_LUT) {
+        const int n_e = d.lut_entries;
+        for (int i = threadIdx.x; i < n_e; i += blockDim.x) {
+            const uint32_t v = a2_eval((uint32_t)i, d.dp);
+            if (d.ob == 2) {
+                // stored byte-swapped so a little-endian u16 store yields PNG order
+                reinterpret_cast<uint16_t*>(d.lut)[i] = (uint16_t)(((v & 0xFF) << 8) | (v >> 8));
+            } else {
+                d.lut[i] = (uint8_t)v;
+            }
+        }
+    } else if (mode == W_LUT8) {
+        const int n_e = d.lut_entries;
+        for (int i = threadIdx.x; i < n_e; i += blockDim.x) d.lut[i] = lut8_eval(i, n_e, d.dp);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused window + filter
+// ---------------------------------------------------------------------------
+constexpr int kFiltThreads = 256;
+constexpr int kFiltWarps = kFiltThreads / 32;
+
+__host__ __device__ inline int warps_per_row(int rb)
+{
+    return rb <= 4096 ? 1 : rb <= 8192 ? 2 : rb <= 16384 ? 4 : 8;
+}
+
+__host__ __device__ inline int slot_stride(int rb)
+{
+    return 16 + ((rb + 15) & ~15) + 16;
+}
+
+__host__ __device__ inline int lut_region_bytes(int mode, int entries, int esize)
+{
+    const bool lut = (mode == W_A2_LUT) || (mode == W_LUT8);
+    const int b = entries * esize;
+    return (lut && b <= kMaxSmemLut) ? ((b + 15) & ~15) : 0;
+}
+
+struct WinCtx {
+    int mode, ib, ob, shift;
+    uint32_t mask;
+    int32_t qa, qb;
+    const uint8_t* lut;         // shared or global table
+    r2p_dicom_params dp;
+};
+
+__device__ __forceinline__ uint32_t lut_get(const WinCtx& w, uint32_t idx)
+{
+    if (w.ob == 2) return reinterpret_cast<const uint16_t*>(w.lut)[idx];
+    return w.lut[idx];
+}
+
+// Window one 16-bit LE sample to an 8-bit output value (Q15 / LUT8 modes).
+__device__ __forceinline__ uint32_t win8(const WinCtx& w, uint32_t raw)
+{
+    if (w.mode == W_Q15) {
+        const int32_t x = (w.dp.pixel_rep == 1) ? (int32_t)(int16_t)(uint16_t)raw : (int32_t)raw;
+        const int32_t v = (int32_t)((uint32_t)x * (uint32_t)w.qa + (uint32_t)w.qb) >> 15;
+        return (uint32_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+    }
+    return w.lut[(raw >> w.shift) & w.mask];
+}
+
+// Window one sample with output depth = input depth; result in PNG byte order
+// packed in the low ob bytes (16-bit: byte 0 = MSB).
+__device__ __forceinline__ uint32_t winN(const WinCtx& w, uint32_t raw)
+{
+    switch (w.mode) {
+        case W_COPY: return raw;                                   // raw already in memory order
+        case W_SWAP16: return ((raw & 0xFF) << 8) | (raw >> 8);
+        case W_A2_LUT: return lut_get(w, win_index(raw, w.shift, w.mask));
+        default: {                                                 // W_A2_DIRECT
+            uint32_t m = raw;
+            if (w.ib == 2) m = win_index(raw, w.shift, w.mask);
+            const uint32_t v = a2_eval(m, w.dp);
+            return (w.ob == 2) ? (((v & 0xFF) << 8) | (v >> 8)) : v;
+        }
+    }
+}
+
+// Window raw row `r` of image d into smem row `dst` (rb bytes) and zero its tail.
+__device__ void window_row_range(const DevImage& d, const WinCtx& w, int r, uint8_t* dst, int tid,
+                                 int nthr, bool aligned)
+{
+    const uint8_t* src = d.raw + (size_t)r * (size_t)d.in_pitch;
+    if (aligned) {
+        const int units = d.in_pitch >> 4;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        for (int u = tid; u < units; u += nthr) {
+            const uint4 v = __ldg(s4 + u);
+            const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+            if (w.ob == w.ib) {
+                uint32_t o[4];
+                if (w.mode == W_COPY) {
+                    o[0] = wv[0]; o[1] = wv[1]; o[2] = wv[2]; o[3] = wv[3];
+                } else if (w.ib == 2) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const uint32_t lo = winN(w, wv[k] & 0xFFFF);
+                        const uint32_t hi = winN(w, wv[k] >> 16);
+                        o[k] = lo | (hi << 16);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        uint32_t acc = 0;
+#pragma unroll
+                        for (int j = 0; j < 4; j++) acc |= winN(w, (wv[k] >> (8 * j)) & 0xFF) << (8 * j);
+                        o[k] = acc;
+                    }
+                }
+                *reinterpret_cast<uint4*>(dst + 16 * u) = make_uint4(o[0], o[1], o[2], o[3]);
+            } else {
+                uint32_t o[2];
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const uint32_t s0 = win8(w, wv[2 * k] & 0xFFFF), s1 = win8(w, wv[2 * k] >> 16);
+                    const uint32_t s2 = win8(w, wv[2 * k + 1] & 0xFFFF), s3 = win8(w, wv[2 * k + 1] >> 16);
+                    o[k] = s0 | (s1 << 8) | (s2 << 16) | (s3 << 24);
+                }
+                *reinterpret_cast<uint2*>(dst + 8 * u) = make_uint2(o[0], o[1]);
+            }
+        }
+    } else {
+        // Any alignment: one output byte group of 4 per thread, byte loads.
+        const int groups = (d.rb + 3) >> 2;
+        for (int g = tid; g < groups; g += nthr) {
+            uint32_t o = 0;
+            const int b0 = 4 * g;
+            if (w.ob == w.ib) {
+                if (w.ib == 2) {
+#pragma unroll
+                    for (int j = 0; j < 2; j++) {
+                        const int bo = b0 + 2 * j;
+                        if (bo < d.rb) {
+                            const uint32_t raw = (uint32_t)__ldg(src + bo) | ((uint32_t)__ldg(src + bo + 1) << 8);
+                            o |= winN(w, raw) << (16 * j);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const int bo = b0 + j;
+                        if (bo < d.rb) o |= winN(w, __ldg(src + bo)) << (8 * j);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int so = 2 * (b0 + j);
+                    if (b0 + j < d.rb) {
+                        const uint32_t raw = (uint32_t)__ldg(src + so) | ((uint32_t)__ldg(src + so + 1) << 8);
+                        o |= win8(w, raw) << (8 * j);
+                    }
+                }
+            }
+            if (b0 + 4 <= d.rb) {
+                *reinterpret_cast<uint32_t*>(dst + b0) = o;
+            } else {
+                for (int j = 0; b0 + j < d.rb; j++) dst[b0 + j] = (uint8_t)(o >> (8 * j));
+            }
+        }
+    }
+    // zero the tail so the last partial word and the word after it read zeros
+    const int tail0 = d.rb, tail1 = ((d.rb + 15) & ~15) + 16;
+    for (int i = tail0 + tid; i < tail1; i += nthr) dst[i] = 0;
+}
+
+// Row words: X = current row, U = row above; word k covers bytes 4k..4k+3.
+__device__ __forceinline__ void load_xabc(const uint32_t* X, const uint32_t* U, int k, int bpp,
+                                          uint32_t& x, uint32_t& a, uint32_t& b, uint32_t& c)
+{
+    const int off = 4 * k - bpp;
+    const int w0 = off >> 2;                 // floor division (guard words cover w0 >= -2)
+    const uint32_t sh = (uint32_t)(off & 3) << 3;
+    x = X[k];
+    b = U[k];
+    a = fshr(X[w0], X[w0 + 1], sh);
+    c = fshr(U[w0], U[w0 + 1], sh);
+}
+
+__device__ __forceinline__ uint8_t filtered_byte(const uint8_t* xr, const uint8_t* ur, int i, int bpp, int f)
+{
+    const uint32_t x = xr[i], b = ur[i];
+    const uint32_t a = (i >= bpp) ? xr[i - bpp] : 0u, c = (i >= bpp) ? ur[i - bpp] : 0u;
+    return (uint8_t)filter_word(f, x, a, b, c);
+}
+
+__global__ void __launch_bounds__(kFiltThreads)
+k_window_filter(const DevImage* __restrict__ imgs, const BandItem* __restrict__ items, int nitems,
+                int smem_bytes)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint32_t red[kFiltWarps][5];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const BandItem bi = items[it];
+        const DevImage& d = imgs[bi.img];
+        const int rb = d.rb, bpp = d.bpp;
+        const int lreg = lut_region_bytes(d.mode, d.lut_entries, d.lut_esize);
+        const int stride = slot_stride(rb);
+        const int G = warps_per_row(rb);
+        const int rpp = kFiltWarps / G;                     // rows per pass
+        int slots = (smem_bytes - lreg) / stride;
+        if (slots > 2 * rpp + 1) slots = 2 * rpp + 1;
+        const int T = slots - 1;                            // rows per tile
+        uint8_t* ring = smem + lreg;
+
+        WinCtx w;
+        w.mode = d.mode; w.ib = d.ib; w.ob = d.ob; w.shift = d.lut_shift; w.mask = d.lut_mask;
+        w.qa = d.qa; w.qb = d.qb; w.dp = d.dp;
+        w.lut = (lreg > 0) ? smem : d.lut;
+
+        __syncthreads();   // previous item finished with shared memory
+        if (lreg > 0) {
+            const uint4* s = reinterpret_cast<const uint4*>(d.lut);
+            uint4* t = reinterpret_cast<uint4*>(smem);
+            for (int i = tid; i < lreg / 16; i += kFiltThreads) t[i] = s[i];
+        }
+        // zero the front guard of every slot
+        for (int i = tid; i < slots * 4; i += kFiltThreads)
+            reinterpret_cast<uint32_t*>(ring + (i >> 2) * stride)[i & 3] = 0u;
+        __syncthreads();
+
+        const bool aligned = ((d.in_pitch & 15) == 0) && ((reinterpret_cast<uintptr_t>(d.raw) & 15) == 0);
+        // row above the band: windowed raw row, caller's prior row, or zeros
+        {
+            uint8_t* dst = ring + 16;                        // slot of rel 0
+            const int r = (int)bi.r0 - 1;
+            if (r >= 0) {
+                window_row_range(d, w, r, dst, tid, kFiltThreads, aligned);
+            } else {
+                const int tail1 = ((rb + 15) & ~15) + 16;
+                for (int i = tid; i < tail1; i += kFiltThreads)
+                    dst[i] = (d.prior && i < rb) ? d.prior[i] : 0;
+            }
+        }
+
+        for (int t0 = (int)bi.r0; t0 < (int)bi.r1; t0 += T) {
+            const int n = min(T, (int)bi.r1 - t0);
+            const int rel0 = t0 - (int)bi.r0 + 1;            // rel of the tile's first row
+            // window the tile's rows: warps take rows round-robin
+            for (int j = warp; j < n; j += kFiltWarps) {
+                uint8_t* dst = ring + ((rel0 + j) % slots) * stride + 16;
+                window_row_range(d, w, t0 + j, dst, lane, 32, aligned);
+            }
+            __syncthreads();
+
+            const int nwords = (rb + 3) >> 2;
+            const int g = warp / G, wg = warp % G;
+            int seg = (nwords + G - 1) / G;
+            seg = (seg + 31) & ~31;
+            const int ws = wg * seg, we = min(nwords, ws + seg);
+            for (int pass = 0; pass * rpp < n; pass++) {
+                const int j = pass * rpp + g;                // tile row index of this group
+                const bool active = j < n;
+                const int rel = rel0 + j;
+                const uint8_t* xr = ring + (rel % slots) * stride + 16;
+                const uint8_t* ur = ring + ((rel - 1 + slots) % slots) * stride + 16;
+                const uint32_t* X = reinterpret_cast<const uint32_t*>(xr);
+                const uint32_t* U = reinterpret_cast<const uint32_t*>(ur);
+                Score5 s = {0u, 0u, 0u, 0u, 0u};
+                if (active) {
+                    const uint32_t tailmask = (rb & 3) ? ((1u << (8 * (rb & 3))) - 1u) : 0xFFFFFFFFu;
+                    for (int k = ws + lane; k < we; k += 32) {
+                        uint32_t x, a, b, c;
+                        load_xabc(X, U, k, bpp, x, a, b, c);
+                        score_word(s, x, a, b, c, (k == nwords - 1) ? tailmask : 0xFFFFFFFFu);
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    s.s0 += __shfl_xor_sync(0xFFFFFFFFu, s.s0, o);
+                    s.s1 += __shfl_xor_sync(0xFFFFFFFFu, s.s1, o);
+                    s.s2 += __shfl_xor_sync(0xFFFFFFFFu, s.s2, o);
+                    s.s3 += __shfl_xor_sync(0xFFFFFFFFu, s.s3, o);
+                    s.s4 += __shfl_xor_sync(0xFFFFFFFFu, s.s4, o);
+                }
+                if (G > 1) {
+                    if (lane == 0) {
+                        red[warp][0] = s.s0; red[warp][1] = s.s1; red[warp][2] = s.s2;
+                        red[warp][3] = s.s3; red[warp][4] = s.s4;
+                    }
+                    __syncthreads();
+                    Score5 t = {0u, 0u, 0u, 0u, 0u};
+                    for (int q = g * G; q < g * G + G; q++) {
+                        t.s0 += red[q][0]; t.s1 += red[q][1]; t.s2 += red[q][2];
+                        t.s3 += red[q][3]; t.s4 += red[q][4];
+                    }
+                    s = t;
+                    __syncthreads();
+                }
+                if (!active) continue;
+                const int f = best_filter(s);
+                const int r = t0 + j;
+                uint8_t* orow = d.filt + (size_t)r * (size_t)(rb + 1);
+                const uintptr_t data_addr = reinterpret_cast<uintptr_t>(orow + 1);
+                const int e = (int)(data_addr & 3);
+                uint32_t* gw = reinterpret_cast<uint32_t*>(data_addr - (uintptr_t)e);   // global word of data byte 0
+                // interior words: k in [klo, khi]
+                const int klo = (e > 0) ? 1 : 0;
+                const int khi = (e + rb - 4) >> 2;
+                uint32_t carry = 0;
+                if (ws > 0) {
+                    uint32_t x, a, b, c;
+                    load_xabc(X, U, ws - 1, bpp, x, a, b, c);
+                    carry = filter_word(f, x, a, b, c);
+                }
+                for (int k0 = ws; k0 < we; k0 += 32) {
+                    const int k = k0 + lane;
+                    uint32_t F = 0;
+                    if (k < we) {
+                        uint32_t x, a, b, c;
+                        load_xabc(X, U, k, bpp, x, a, b, c);
+                        F = filter_word(f, x, a, b, c);
+                    }
+                    uint32_t Fp = __shfl_up_sync(0xFFFFFFFFu, F, 1);
+                    const uint32_t last = __shfl_sync(0xFFFFFFFFu, F, 31);
+                    if (lane == 0) Fp = carry;
+                    carry = last;
+                    if (k < we && k >= klo && k <= khi) {
+                        gw[k] = e ? __funnelshift_l(Fp, F, 8u * (uint32_t)e) : F;
+                    }
+                }
+                // type byte, head bytes before the first interior word, tail bytes after the last
+                if (wg == 0 && lane == 0) {
+                    orow[0] = (uint8_t)f;
+                    const int head = (e > 0) ? min(4 - e, rb) : 0;
+                    for (int i = 0; i < head; i++) orow[1 + i] = filtered_byte(xr, ur, i, bpp, f);
+                }
+                if (wg == G - 1 && lane == 31) {
+                    const int head = (e > 0) ? min(4 - e, rb) : 0;
+                    const int tail_start = max(head, (khi >= klo) ? 4 * (khi + 1) - e : head);
+                    for (int i = tail_start; i < rb; i++) orow[1 + i] = filtered_byte(xr, ur, i, bpp, f);
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace r2p
+
+namespace r2p {
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+constexpr int kFilterSmemCap = 226 * 1024;   // below the 227 KB opt-in limit minus static smem
+
+int filter_lut_region(int mode, int lut_entries, int lut_esize)
+{
+    return lut_region_bytes(mode, lut_entries, lut_esize);
+}
+
+// Dynamic shared memory wanted for an image: LUT region plus 2*rows_per_pass+1
+// row slots (fewer when rows are wide); -1 when not even two slots fit.
+int filter_smem_bytes(int rb, int mode, int lut_entries, int lut_esize)
+{
+    const int lreg = lut_region_bytes(mode, lut_entries, lut_esize);
+    const int stride = slot_stride(rb);
+    const int rpp = kFiltWarps / warps_per_row(rb);
+    int slots = 2 * rpp + 1;
+    if (lreg + slots * stride > kFilterSmemCap) slots = (kFilterSmemCap - lreg) / stride;
+    if (slots < 2) return -1;
+    return lreg + slots * stride;
+}
+
+int filter_tile_rows(int rb, int smem, int lut_region)
+{
+    const int stride = slot_stride(rb);
+    const int rpp = kFiltWarps / warps_per_row(rb);
+    int slots = (smem - lut_region) / stride;
+    if (slots > 2 * rpp + 1) slots = 2 * rpp + 1;
+    return slots - 1;
+}
+
+int filter_ctas_per_sm(int smem)
+{
+    int n = 0;
+    cudaFuncSetAttribute(k_window_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, kFilterSmemCap);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_window_filter, kFiltThreads, smem) != cudaSuccess)
+        return 1;
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s)
+{
+    k_prepare_window<<<n, 256, 0, s>>>(imgs, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_window_filter(const DevImage* imgs, const BandItem* items, int nitems, int grid, int smem,
+                                 cudaStream_t s)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_window_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kFilterSmemCap);
+    if (e != cudaSuccess) return e;
+    k_window_filter<<<grid, kFiltThreads, smem, s>>>(imgs, items, nitems, smem);
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace r2p

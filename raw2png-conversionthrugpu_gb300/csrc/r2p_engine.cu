@@ -1,0 +1,726 @@
+// r2p_engine.cu -- host side of the encoder: the C ABI of include/r2p.h.
+//
+// An engine owns one device's scratch memory (a reusable arena), a pinned
+// staging area for work descriptors, and the CRC power table.  Every encode
+// call builds a plan on the host (per image: geometry, window request, row
+// bands for the filter kernel, DEFLATE blocks), uploads it in one copy, and
+// launches one kernel per stage over the whole work list:
+//   k_prepare_window -> k_window_filter -> k_stored_blocks | k_lz77_blocks
+//   -> k_finalize -> (k_copy_blocks)
+// Calls are ordered through the engine: each call waits (on the device, not
+// the host) for the previous call's last kernel before reusing the arena.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "r2p_common.h"
+#include "r2p_device.h"
+#include "r2p_kernels.h"
+
+namespace r2p {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+static thread_local std::string t_last_error;
+
+static int set_err(int code, const char* what)
+{
+    t_last_error = what ? what : "";
+    return code;
+}
+
+static int cuda_err(cudaError_t e, const char* where)
+{
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+    t_last_error = buf;
+    return e == cudaErrorMemoryAllocation ? R2P_ENOMEM : R2P_ECUDA;
+}
+
+#define R2P_CU(call, where)                                     \
+    do {                                                        \
+        cudaError_t _e = (call);                                \
+        if (_e != cudaSuccess) return cuda_err(_e, where);      \
+    } while (0)
+
+static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// x^(8 * j * 2^(10 l)) mod P, l = 0..3, j = 0..1023 (see xpow8n)
+static void build_xpow(std::vector<uint32_t>& tab)
+{
+    tab.assign(kXpowLevels * 1024, 0);
+    uint32_t base = 1u << 23;   // x^8
+    for (int l = 0; l < kXpowLevels; l++) {
+        uint32_t v = 0x80000000u;   // x^0
+        for (int j = 0; j < 1024; j++) {
+            tab[l * 1024 + j] = v;
+            v = gf2_mulmod(v, base);
+        }
+        for (int k = 0; k < 10; k++) base = gf2_mulmod(base, base);   // base^1024
+    }
+}
+
+// ---------------------------------------------------------------------------
+// planning
+// ---------------------------------------------------------------------------
+struct ImgPlan {
+    DevImage di;
+    uint64_t raw_bytes = 0;
+    uint64_t lut_cap = 0;
+    uint64_t png_bound = 0;
+    int smem = 0;      // filter smem wanted
+    int lreg = 0;      // worst-case LUT region
+};
+
+static int auto_block_size(const r2p_image& im, uint64_t F)
+{
+    (void)im;
+    (void)F;
+    return kBlock64;
+}
+
+static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip)
+{
+    if (im.width < 1 || im.height < 1) return set_err(R2P_EINVAL, "width and height must be >= 1");
+    if (im.channels != 1 && im.channels != 3 && im.channels != 4)
+        return set_err(R2P_EINVAL, "channels must be 1, 3 or 4");
+    if (im.bytes_per_sample != 1 && im.bytes_per_sample != 2)
+        return set_err(R2P_EINVAL, "bytes_per_sample must be 1 or 2");
+    if (im.level < 0 || im.level > 9) return set_err(R2P_EINVAL, "level must be 0..9");
+    const r2p_dicom_params& p = im.dicom;
+    int ob = im.bytes_per_sample;
+    switch (im.window_mode) {
+        case R2P_WINDOW_NONE:
+            break;
+        case R2P_WINDOW_SWAP16:
+            if (im.bytes_per_sample != 2) return set_err(R2P_EINVAL, "SWAP16 needs 16-bit samples");
+            break;
+        case R2P_WINDOW_DICOM16:
+            if (p.bits_allocated != 8 * im.bytes_per_sample)
+                return set_err(R2P_EINVAL, "DICOM16: bits_allocated must match bytes_per_sample");
+            if (p.bits_stored < 1 || p.bits_stored > p.bits_allocated)
+                return set_err(R2P_EINVAL, "DICOM16: bits_stored out of range");
+            break;
+        case R2P_WINDOW_BATCH8:
+            if (im.bytes_per_sample != 2 || im.channels != 1)
+                return set_err(R2P_EINVAL, "BATCH8 needs 16-bit grayscale samples");
+            if (p.bits_stored < 1 || p.bits_stored > 16 || p.high_bit - p.bits_stored + 1 < 0 ||
+                p.high_bit > 15)
+                return set_err(R2P_EINVAL, "BATCH8: bits_stored/high_bit out of range");
+            ob = 1;
+            break;
+        default:
+            return set_err(R2P_EINVAL, "unknown window_mode");
+    }
+    DevImage& d = ip.di;
+    memset(&d, 0, sizeof(d));
+    d.width = im.width;
+    d.height = im.height;
+    d.channels = im.channels;
+    d.ib = im.bytes_per_sample;
+    d.ob = ob;
+    const uint64_t rb = (uint64_t)im.width * im.channels * ob;
+    const uint64_t pitch = (uint64_t)im.width * im.channels * im.bytes_per_sample;
+    if (rb > (1u << 20)) return set_err(R2P_EINVAL, "row too wide");
+    d.rb = (int32_t)rb;
+    d.bpp = im.channels * ob;
+    d.in_pitch = (int32_t)pitch;
+    const uint64_t F = (uint64_t)im.height * (rb + 1);
+    d.filt_bytes = F;
+    d.req_mode = im.window_mode;
+    d.dp = im.dicom;
+    d.level = im.level;
+    int bs = im.block_size ? im.block_size : auto_block_size(im, F);
+    if (bs < 1024 || bs > kBlock64 || (bs & 15)) return set_err(R2P_EINVAL, "block_size must be a multiple of 16 in [1024, 65520]");
+    d.block_size = bs;
+    const uint64_t nb = (F + bs - 1) / bs;
+    d.nblocks = (int32_t)nb;
+    d.out_kind = out_kind;
+    d.prefix = out_kind == 0 ? kPngPrefix : 2;
+    ip.raw_bytes = pitch * im.height;
+    // worst-case table for the window request (resolved on the device)
+    int entries = 0, esize = 0, mode_guess = W_COPY;
+    if (im.window_mode == R2P_WINDOW_DICOM16) {
+        entries = (im.bytes_per_sample == 2) ? (p.bits_stored < 16 ? (1 << p.bits_stored) : 65536) : 256;
+        esize = ob;
+        mode_guess = W_A2_LUT;
+    } else if (im.window_mode == R2P_WINDOW_BATCH8) {
+        entries = 1 << p.bits_stored;
+        esize = 1;
+        mode_guess = W_LUT8;
+    }
+    ip.lut_cap = align_up((uint64_t)entries * esize + 16, 256);
+    ip.lreg = filter_lut_region(mode_guess, entries, esize);
+    ip.smem = filter_smem_bytes(d.rb, mode_guess, entries, esize);
+    if (ip.smem < 0) return set_err(R2P_EINVAL, "row too wide for the filter kernel");
+    ip.png_bound = (uint64_t)d.prefix + F + (uint64_t)kStoredHdr * nb + (out_kind == 0 ? kPngSuffix : 4);
+    if (F >= (1ull << 32) || ip.png_bound >= (1ull << 31) - 64)
+        return set_err(R2P_EINVAL, "image too large for a single IDAT chunk");
+    return R2P_OK;
+}
+
+}  // namespace r2p
+
+using namespace r2p;
+
+struct r2p_engine {
+    int device = 0;
+    size_t budget = 0;
+    int nsm = 1;
+    uint32_t* d_xpow = nullptr;
+    uint8_t* arena = nullptr;
+    size_t arena_cap = 0;
+    uint8_t* h_stage = nullptr;
+    size_t stage_cap = 0;
+    cudaEvent_t done = nullptr;     // last kernel of the previous call
+    cudaEvent_t staged = nullptr;   // descriptor upload of the previous call
+    bool have_done = false;
+    std::mutex mu;
+};
+
+namespace r2p {
+
+// Bump allocator over one plan's arena layout.
+struct Layout {
+    size_t off = 0;
+    size_t take(size_t bytes)
+    {
+        const size_t o = off;
+        off = align_up(off + bytes, 256);
+        return o;
+    }
+};
+
+struct CallBuffers {
+    // per image, caller-provided or arena
+    std::vector<const uint8_t*> raw;
+    std::vector<uint8_t*> filt;
+    std::vector<const uint8_t*> prior;
+    std::vector<uint8_t*> out;
+    std::vector<uint64_t> out_cap;
+    std::vector<uint64_t*> out_len;
+};
+
+enum Stages { ST_FILTER = 1, ST_DEFLATE = 2, ST_ALL = 3 };
+
+static int ensure_arena(r2p_engine* e, size_t need)
+{
+    if (need <= e->arena_cap) return R2P_OK;
+    if (e->budget && need > e->budget) return set_err(R2P_EBUDGET, "request exceeds the engine's HBM budget");
+    if (e->have_done) R2P_CU(cudaEventSynchronize(e->done), "arena wait");
+    if (e->arena) cudaFree(e->arena);
+    e->arena = nullptr;
+    e->arena_cap = 0;
+    size_t cap = align_up(need + need / 4, 1 << 20);
+    if (e->budget && cap > e->budget) cap = need;
+    R2P_CU(cudaMalloc(&e->arena, cap), "arena cudaMalloc");
+    e->arena_cap = cap;
+    return R2P_OK;
+}
+
+static int ensure_stage(r2p_engine* e, size_t need)
+{
+    if (e->have_done) R2P_CU(cudaEventSynchronize(e->staged), "staging wait");
+    if (need <= e->stage_cap) return R2P_OK;
+    if (e->h_stage) cudaFreeHost(e->h_stage);
+    e->h_stage = nullptr;
+    size_t cap = align_up(need * 2, 1 << 16);
+    R2P_CU(cudaMallocHost(&e->h_stage, cap), "staging cudaMallocHost");
+    e->stage_cap = cap;
+    return R2P_OK;
+}
+
+// One call's work list and arena layout.
+struct Prepared {
+    std::vector<BandItem> items;
+    std::vector<BlockOut> blocks;
+    int smem = 0, slots_total = 0, max_block = 0;
+    uint32_t nblk = 0;
+    bool any_lz = false, any_stored = false;
+    uint64_t slot = 0;
+    size_t o_img = 0, o_items = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0, o_extra = 0;
+};
+
+// Plan the work list and arena layout for n images, make sure the arena and
+// staging area are large enough, and order this call after the previous one
+// on `s`.  *extra receives extra_bytes of arena space for the caller.
+static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
+                   cudaStream_t s, Prepared& P, uint8_t** extra)
+{
+    const int n = (int)plans.size();
+    for (auto& p : plans) P.smem = std::max(P.smem, p.smem);
+    const int cps = P.smem > 0 ? filter_ctas_per_sm(P.smem) : 1;
+    P.slots_total = e->nsm * cps;
+    uint64_t lut_total = 0, filt_total = 0;
+    for (int i = 0; i < n; i++) {
+        DevImage& d = plans[i].di;
+        if (P.smem > 0) {
+            const int T = filter_tile_rows(d.rb, P.smem, plans[i].lreg);
+            const uint64_t ntiles = (d.height + T - 1) / T;
+            uint64_t nb = std::min<uint64_t>(ntiles, (uint64_t)P.slots_total);
+            if (n > 1) nb = std::min<uint64_t>(ntiles, std::max<uint64_t>(1, (uint64_t)P.slots_total / n + 1));
+            const uint64_t band_rows = ((ntiles + nb - 1) / nb) * T;
+            for (uint64_t r = 0; r < d.height; r += band_rows)
+                P.items.push_back(BandItem{(uint32_t)i, (uint32_t)r,
+                                           (uint32_t)std::min<uint64_t>(d.height, r + band_rows)});
+        }
+        d.blk0 = P.nblk;
+        for (int k = 0; k < d.nblocks; k++) {
+            BlockOut bo;
+            memset(&bo, 0, sizeof(bo));
+            bo.img = (uint32_t)i;
+            bo.in_off = (uint32_t)((uint64_t)k * d.block_size);
+            bo.in_len = (uint32_t)std::min<uint64_t>(d.block_size, d.filt_bytes - (uint64_t)k * d.block_size);
+            P.blocks.push_back(bo);
+        }
+        P.nblk += (uint32_t)d.nblocks;
+        P.max_block = std::max(P.max_block, d.block_size);
+        if (d.level == 0) P.any_stored = true; else P.any_lz = true;
+        lut_total += plans[i].lut_cap;
+        if (!cb.filt[i]) filt_total += align_up(d.filt_bytes + 64, 256);
+    }
+    P.slot = P.any_lz ? lz77_slot_bytes(P.max_block) : 0;
+    Layout L;
+    P.o_img = L.take(sizeof(DevImage) * n);
+    P.o_items = L.take(sizeof(BandItem) * std::max<size_t>(1, P.items.size()));
+    P.o_blocks = L.take(sizeof(BlockOut) * std::max<size_t>(1, P.blocks.size()));
+    P.desc_bytes = L.off;
+    P.o_lut = L.take(lut_total);
+    P.o_filt = L.take(filt_total);
+    P.o_scratch = L.take(P.slot * P.nblk);
+    P.o_extra = L.take(extra_bytes);
+    int rc = ensure_arena(e, L.off);
+    if (rc) return rc;
+    rc = ensure_stage(e, P.desc_bytes);
+    if (rc) return rc;
+    if (e->have_done) R2P_CU(cudaStreamWaitEvent(s, e->done, 0), "order calls");
+    if (extra) *extra = e->arena + P.o_extra;
+    return R2P_OK;
+}
+
+// Fill the device pointers, upload the descriptors and launch the stages.
+static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, Prepared& P, int stages,
+                  cudaStream_t s)
+{
+    const int n = (int)plans.size();
+    uint8_t* A = e->arena;
+    uint64_t lut_off = P.o_lut, filt_off = P.o_filt;
+    for (int i = 0; i < n; i++) {
+        DevImage& d = plans[i].di;
+        d.lut = A + lut_off;
+        lut_off += plans[i].lut_cap;
+        d.raw = cb.raw[i];
+        d.prior = cb.prior[i];
+        if (cb.filt[i]) {
+            d.filt = cb.filt[i];
+        } else {
+            d.filt = A + filt_off;
+            filt_off += align_up(d.filt_bytes + 64, 256);
+        }
+        d.png = cb.out[i];
+        d.png_cap = cb.out_cap[i];
+        d.png_len = cb.out_len[i];
+    }
+    uint8_t* H = e->h_stage;
+    for (int i = 0; i < n; i++) memcpy(H + P.o_img + i * sizeof(DevImage), &plans[i].di, sizeof(DevImage));
+    if (!P.items.empty()) memcpy(H + P.o_items, P.items.data(), P.items.size() * sizeof(BandItem));
+    if (!P.blocks.empty()) memcpy(H + P.o_blocks, P.blocks.data(), P.blocks.size() * sizeof(BlockOut));
+    R2P_CU(cudaMemcpyAsync(A, H, P.desc_bytes, cudaMemcpyHostToDevice, s), "descriptor upload");
+    R2P_CU(cudaEventRecord(e->staged, s), "event");
+    DevImage* dimg = reinterpret_cast<DevImage*>(A + P.o_img);
+    BandItem* ditems = reinterpret_cast<BandItem*>(A + P.o_items);
+    BlockOut* dblocks = reinterpret_cast<BlockOut*>(A + P.o_blocks);
+    if (stages & ST_FILTER) {
+        R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
+        const int grid = (int)std::min<size_t>(P.items.size(), (size_t)P.slots_total);
+        R2P_CU(launch_window_filter(dimg, ditems, (int)P.items.size(), grid, P.smem, s), "k_window_filter");
+    }
+    if (stages & ST_DEFLATE) {
+        const int grid = (int)std::min<uint64_t>(P.nblk, (uint64_t)e->nsm * 8);
+        if (P.any_stored)
+            R2P_CU(launch_stored(dimg, dblocks, (int)P.nblk, P.max_block, e->d_xpow, grid, s), "k_stored_blocks");
+        if (P.any_lz)
+            R2P_CU(launch_lz77(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, grid, s),
+                   "k_lz77_blocks");
+        R2P_CU(launch_finalize(dimg, n, dblocks, e->d_xpow, s), "k_finalize");
+        if (P.any_lz)
+            R2P_CU(launch_copy_blocks(dimg, dblocks, (int)P.nblk, A + P.o_scratch, P.slot, grid, s), "k_copy_blocks");
+    }
+    R2P_CU(cudaEventRecord(e->done, s), "event");
+    e->have_done = true;
+    return R2P_OK;
+}
+
+static int run(r2p_engine* e, std::vector<ImgPlan>& plans, CallBuffers& cb, int stages, cudaStream_t s)
+{
+    Prepared P;
+    int rc = prepare(e, plans, cb, 0, s, P, nullptr);
+    if (rc) return rc;
+    return launch(e, plans, cb, P, stages, s);
+}
+
+static int bind(r2p_engine* e)
+{
+    R2P_CU(cudaSetDevice(e->device), "cudaSetDevice");
+    return R2P_OK;
+}
+
+}  // namespace r2p
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int r2p_version(void) { return 10000; }
+
+const char* r2p_status_string(int st)
+{
+    switch (st) {
+        case R2P_OK: return "ok";
+        case R2P_EINVAL: return "invalid argument";
+        case R2P_ENOMEM: return "out of memory";
+        case R2P_EBUDGET: return "HBM budget exceeded";
+        case R2P_ECUDA: return "CUDA error";
+        case R2P_ETIMEOUT: return "timed out";
+        case R2P_ENOSPC: return "output buffer too small";
+        case R2P_ECANCELED: return "cancelled";
+        case R2P_ENOTFOUND: return "unknown ticket";
+        default: return "unknown status";
+    }
+}
+
+const char* r2p_last_error(void) { return t_last_error.c_str(); }
+
+uint64_t r2p_kernel_launch_count(void) { return g_launches.load(); }
+
+int r2p_engine_create(int device, size_t hbm_budget, r2p_engine** out)
+{
+    if (!out) return set_err(R2P_EINVAL, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    R2P_CU(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) return set_err(R2P_EINVAL, "no such device");
+    r2p_engine* e = new r2p_engine();
+    e->device = device;
+    e->budget = hbm_budget;
+    cudaError_t ce = cudaSetDevice(device);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, device);
+    std::vector<uint32_t> tab;
+    build_xpow(tab);
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_xpow, tab.size() * 4);
+    if (ce == cudaSuccess) ce = cudaMemcpy(e->d_xpow, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->staged, cudaEventDisableTiming);
+    if (ce != cudaSuccess) {
+        r2p_engine_destroy(e);
+        return cuda_err(ce, "r2p_engine_create");
+    }
+    *out = e;
+    return R2P_OK;
+}
+
+void r2p_engine_destroy(r2p_engine* e)
+{
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->have_done) cudaEventSynchronize(e->done);
+    if (e->arena) cudaFree(e->arena);
+    if (e->d_xpow) cudaFree(e->d_xpow);
+    if (e->h_stage) cudaFreeHost(e->h_stage);
+    if (e->done) cudaEventDestroy(e->done);
+    if (e->staged) cudaEventDestroy(e->staged);
+    delete e;
+}
+
+size_t r2p_png_bound(const r2p_image* img)
+{
+    if (!img) return 0;
+    ImgPlan ip;
+    if (plan_image(*img, 0, ip)) return 0;
+    return (size_t)ip.png_bound;
+}
+
+size_t r2p_zlib_bound(size_t len, int level, int block_size)
+{
+    (void)level;
+    const int bs = block_size ? block_size : kBlock64;
+    if (bs < 1024 || bs > kBlock64 || (bs & 15)) return 0;
+    return 2 + len + (size_t)kStoredHdr * ((len + bs - 1) / bs + 1) + 4;
+}
+
+int r2p_encode_png_device(r2p_engine* e, const r2p_image* img, const void* d_pixels, void* d_png,
+                          size_t png_cap, uint64_t* d_png_len, void* stream)
+{
+    if (!e || !img || !d_pixels || !d_png || !d_png_len) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    std::vector<ImgPlan> plans(1);
+    rc = plan_image(*img, 0, plans[0]);
+    if (rc) return rc;
+    if (png_cap < plans[0].png_bound) return set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
+    CallBuffers cb;
+    cb.raw = {static_cast<const uint8_t*>(d_pixels)};
+    cb.filt = {nullptr};
+    cb.prior = {nullptr};
+    cb.out = {static_cast<uint8_t*>(d_png)};
+    cb.out_cap = {png_cap};
+    cb.out_len = {d_png_len};
+    return run(e, plans, cb, ST_ALL, static_cast<cudaStream_t>(stream));
+}
+
+int r2p_encode_batch_device(r2p_engine* e, int n, const r2p_image* imgs, const void* const* d_pixels,
+                            void* const* d_pngs, const size_t* png_caps, uint64_t* d_png_lens, void* stream)
+{
+    if (!e || n < 1 || !imgs || !d_pixels || !d_pngs || !png_caps || !d_png_lens)
+        return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    std::vector<ImgPlan> plans((size_t)n);
+    CallBuffers cb;
+    for (int i = 0; i < n; i++) {
+        rc = plan_image(imgs[i], 0, plans[i]);
+        if (rc) return rc;
+        if (png_caps[i] < plans[i].png_bound) return set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
+        if (!d_pixels[i] || !d_pngs[i]) return set_err(R2P_EINVAL, "NULL buffer");
+        cb.raw.push_back(static_cast<const uint8_t*>(d_pixels[i]));
+        cb.filt.push_back(nullptr);
+        cb.prior.push_back(nullptr);
+        cb.out.push_back(static_cast<uint8_t*>(d_pngs[i]));
+        cb.out_cap.push_back(png_caps[i]);
+        cb.out_len.push_back(d_png_lens + i);
+    }
+    return run(e, plans, cb, ST_ALL, static_cast<cudaStream_t>(stream));
+}
+
+int r2p_encode_png(r2p_engine* e, const r2p_image* img, const void* h_pixels, void* h_png, size_t png_cap,
+                   size_t* png_len)
+{
+    if (!e || !img || !h_pixels || !h_png || !png_len) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    std::vector<ImgPlan> plans(1);
+    rc = plan_image(*img, 0, plans[0]);
+    if (rc) return rc;
+    const size_t raw_bytes = (size_t)plans[0].raw_bytes;
+    const size_t bound = (size_t)plans[0].png_bound;
+    const size_t raw_region = align_up(raw_bytes + 16, 256), png_region = align_up(bound, 256);
+    CallBuffers cb;
+    cb.raw = {nullptr};
+    cb.filt = {nullptr};
+    cb.prior = {nullptr};
+    cb.out = {nullptr};
+    cb.out_cap = {bound};
+    cb.out_len = {nullptr};
+    cudaStream_t s = 0;
+    Prepared P;
+    uint8_t* ext = nullptr;
+    rc = prepare(e, plans, cb, raw_region + png_region + 256, s, P, &ext);
+    if (rc) return rc;
+    uint8_t* d_raw = ext;
+    uint8_t* d_png = ext + raw_region;
+    uint64_t* d_len = reinterpret_cast<uint64_t*>(d_png + png_region);
+    cb.raw = {d_raw};
+    cb.out = {d_png};
+    cb.out_len = {d_len};
+    R2P_CU(cudaMemcpyAsync(d_raw, h_pixels, raw_bytes, cudaMemcpyHostToDevice, s), "pixel upload");
+    rc = launch(e, plans, cb, P, ST_ALL, s);
+    if (rc) return rc;
+    uint64_t len = 0;
+    R2P_CU(cudaMemcpyAsync(&len, d_len, sizeof(len), cudaMemcpyDeviceToHost, s), "length download");
+    R2P_CU(cudaStreamSynchronize(s), "sync");
+    if (len == ~0ull) return set_err(R2P_ENOSPC, "png buffer too small");
+    *png_len = (size_t)len;
+    if (len > png_cap) return set_err(R2P_ENOSPC, "png_cap too small for the encoded PNG");
+    R2P_CU(cudaMemcpyAsync(h_png, d_png, (size_t)len, cudaMemcpyDeviceToHost, s), "png download");
+    R2P_CU(cudaStreamSynchronize(s), "sync");
+    return R2P_OK;
+}
+
+int r2p_window_filter_device(r2p_engine* e, const r2p_image* img, const void* d_pixels, const void* d_prior,
+                             void* d_filtered, void* stream)
+{
+    if (!e || !img || !d_pixels || !d_filtered) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    std::vector<ImgPlan> plans(1);
+    rc = plan_image(*img, 0, plans[0]);
+    if (rc) return rc;
+    CallBuffers cb;
+    cb.raw = {static_cast<const uint8_t*>(d_pixels)};
+    cb.filt = {static_cast<uint8_t*>(d_filtered)};
+    cb.prior = {static_cast<const uint8_t*>(d_prior)};
+    cb.out = {nullptr};
+    cb.out_cap = {0};
+    cb.out_len = {nullptr};
+    return run(e, plans, cb, ST_FILTER, static_cast<cudaStream_t>(stream));
+}
+
+int r2p_zlib_compress_device(r2p_engine* e, const void* d_in, size_t len, int level, int block_size,
+                             void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream)
+{
+    if (!e || !d_in || !d_out || !d_out_len) return set_err(R2P_EINVAL, "NULL argument");
+    if (len == 0 || len >= (1ull << 31)) return set_err(R2P_EINVAL, "len must be in [1, 2^31)");
+    if (level < 0 || level > 9) return set_err(R2P_EINVAL, "level must be 0..9");
+    const int bs = block_size ? block_size : kBlock64;
+    if (bs < 1024 || bs > kBlock64 || (bs & 15)) return set_err(R2P_EINVAL, "bad block_size");
+    if (out_cap < r2p_zlib_bound(len, level, block_size)) return set_err(R2P_ENOSPC, "out_cap below r2p_zlib_bound()");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    // The bytes are planned as one "image" whose filtered stream is d_in; only
+    // the DEFLATE stages run.
+    std::vector<ImgPlan> plans(1);
+    DevImage& d = plans[0].di;
+    memset(&d, 0, sizeof(d));
+    d.width = 1; d.height = 1; d.channels = 1; d.ib = 1; d.ob = 1; d.rb = 0; d.bpp = 1;
+    d.filt_bytes = len;
+    d.level = level;
+    d.block_size = bs;
+    d.nblocks = (int32_t)((len + bs - 1) / bs);
+    d.out_kind = 1;
+    d.prefix = 2;
+    d.req_mode = R2P_WINDOW_NONE;
+    plans[0].smem = 0;
+    plans[0].lreg = 0;
+    plans[0].lut_cap = 256;
+    CallBuffers cb;
+    cb.raw = {nullptr};
+    cb.filt = {static_cast<uint8_t*>(const_cast<void*>(d_in))};
+    cb.prior = {nullptr};
+    cb.out = {static_cast<uint8_t*>(d_out)};
+    cb.out_cap = {out_cap};
+    cb.out_len = {d_out_len};
+    return run(e, plans, cb, ST_DEFLATE, static_cast<cudaStream_t>(stream));
+}
+
+int r2p_adler32_device(r2p_engine* e, const void* d_data, size_t len, uint32_t* d_result, void* stream)
+{
+    if (!e || (!d_data && len) || !d_result) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    rc = ensure_arena(e, checksum_scratch_bytes(len));
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (e->have_done) R2P_CU(cudaStreamWaitEvent(s, e->done, 0), "order calls");
+    R2P_CU(launch_checksum(static_cast<const uint8_t*>(d_data), len, true, d_result, e->arena, e->d_xpow,
+                           e->nsm * 4, s), "k_checksum");
+    R2P_CU(cudaEventRecord(e->done, s), "event");
+    e->have_done = true;
+    return R2P_OK;
+}
+
+int r2p_crc32_device(r2p_engine* e, const void* d_data, size_t len, uint32_t* d_result, void* stream)
+{
+    if (!e || (!d_data && len) || !d_result) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    rc = ensure_arena(e, checksum_scratch_bytes(len));
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (e->have_done) R2P_CU(cudaStreamWaitEvent(s, e->done, 0), "order calls");
+    R2P_CU(launch_checksum(static_cast<const uint8_t*>(d_data), len, false, d_result, e->arena, e->d_xpow,
+                           e->nsm * 4, s), "k_checksum");
+    R2P_CU(cudaEventRecord(e->done, s), "event");
+    e->have_done = true;
+    return R2P_OK;
+}
+
+uint32_t r2p_crc32_combine(uint32_t crc1, uint32_t crc2, uint64_t len2)
+{
+    static CrcPow pw = [] { CrcPow t; crc_init_pow(t); return t; }();
+    return crc32_combine(crc1, crc2, len2, pw.p);
+}
+
+uint32_t r2p_adler32_combine(uint32_t a1, uint32_t a2, uint64_t len2) { return r2p::adler32_combine(a1, a2, len2); }
+
+int r2p_device_alloc(size_t bytes, void** p)
+{
+    if (!p) return set_err(R2P_EINVAL, "NULL argument");
+    R2P_CU(cudaMalloc(p, bytes ? bytes : 1), "cudaMalloc");
+    return R2P_OK;
+}
+int r2p_device_free(void* p)
+{
+    R2P_CU(cudaFree(p), "cudaFree");
+    return R2P_OK;
+}
+int r2p_host_alloc_pinned(size_t bytes, void** p)
+{
+    if (!p) return set_err(R2P_EINVAL, "NULL argument");
+    R2P_CU(cudaMallocHost(p, bytes ? bytes : 1), "cudaMallocHost");
+    return R2P_OK;
+}
+int r2p_host_free_pinned(void* p)
+{
+    R2P_CU(cudaFreeHost(p), "cudaFreeHost");
+    return R2P_OK;
+}
+int r2p_memcpy(void* dst, const void* src, size_t bytes, void* stream)
+{
+    R2P_CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, static_cast<cudaStream_t>(stream)), "cudaMemcpyAsync");
+    return R2P_OK;
+}
+int r2p_memset_device(void* p, int v, size_t bytes, void* stream)
+{
+    R2P_CU(cudaMemsetAsync(p, v, bytes, static_cast<cudaStream_t>(stream)), "cudaMemsetAsync");
+    return R2P_OK;
+}
+int r2p_stream_create(void** s)
+{
+    if (!s) return set_err(R2P_EINVAL, "NULL argument");
+    cudaStream_t st;
+    R2P_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    *s = st;
+    return R2P_OK;
+}
+int r2p_stream_destroy(void* s)
+{
+    R2P_CU(cudaStreamDestroy(static_cast<cudaStream_t>(s)), "cudaStreamDestroy");
+    return R2P_OK;
+}
+int r2p_stream_synchronize(void* s)
+{
+    R2P_CU(cudaStreamSynchronize(static_cast<cudaStream_t>(s)), "cudaStreamSynchronize");
+    return R2P_OK;
+}
+int r2p_event_create(void** ev)
+{
+    if (!ev) return set_err(R2P_EINVAL, "NULL argument");
+    cudaEvent_t e;
+    R2P_CU(cudaEventCreate(&e), "cudaEventCreate");
+    *ev = e;
+    return R2P_OK;
+}
+int r2p_event_destroy(void* ev)
+{
+    R2P_CU(cudaEventDestroy(static_cast<cudaEvent_t>(ev)), "cudaEventDestroy");
+    return R2P_OK;
+}
+int r2p_event_record(void* ev, void* s)
+{
+    R2P_CU(cudaEventRecord(static_cast<cudaEvent_t>(ev), static_cast<cudaStream_t>(s)), "cudaEventRecord");
+    return R2P_OK;
+}
+int r2p_event_elapsed_ms(void* a, void* b, float* ms)
+{
+    if (!ms) return set_err(R2P_EINVAL, "NULL argument");
+    R2P_CU(cudaEventSynchronize(static_cast<cudaEvent_t>(b)), "cudaEventSynchronize");
+    R2P_CU(cudaEventElapsedTime(ms, static_cast<cudaEvent_t>(a), static_cast<cudaEvent_t>(b)), "cudaEventElapsedTime");
+    return R2P_OK;
+}
+
+}  // extern "C"

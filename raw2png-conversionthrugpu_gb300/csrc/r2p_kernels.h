@@ -1,0 +1,37 @@
+// r2p_kernels.h -- host-side launch wrappers of the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "r2p_device.h"
+
+namespace r2p {
+
+// count of kernels this library launched (all streams)
+void note_launch();
+
+// k_filter.cu
+cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s);
+cudaError_t launch_window_filter(const DevImage* imgs, const BandItem* items, int nitems, int grid,
+                                 int smem, cudaStream_t s);
+int filter_smem_bytes(int rb, int mode, int lut_entries, int lut_esize);
+int filter_tile_rows(int rb, int smem, int lut_region);
+int filter_lut_region(int mode, int lut_entries, int lut_esize);
+int filter_ctas_per_sm(int smem);
+
+// k_deflate.cu
+int stored_smem_bytes(int block_size);
+cudaError_t launch_stored(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block,
+                          const uint32_t* xpow, int grid, cudaStream_t s);
+cudaError_t launch_finalize(DevImage* imgs, int nimg, BlockOut* blocks, const uint32_t* xpow, cudaStream_t s);
+cudaError_t launch_copy_blocks(const DevImage* imgs, const BlockOut* blocks, int nblocks,
+                               const uint8_t* scratch, uint64_t slot_bytes, int grid, cudaStream_t s);
+size_t checksum_scratch_bytes(uint64_t len);
+cudaError_t launch_checksum(const uint8_t* data, uint64_t len, bool adler, uint32_t* result, void* scratch,
+                            const uint32_t* xpow, int grid, cudaStream_t s);
+
+// k_lz77.cu
+uint64_t lz77_slot_bytes(int block_size);
+cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
+                        uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s);
+
+}  // namespace r2p

@@ -1,0 +1,176 @@
+"""Window + adaptive filter on the GPU, bit-exact against the oracle.
+
+Each case runs r2p_window_filter_device (C ABI) and compares the filtered
+scanlines -- filter-type bytes and filtered bytes -- with the CPU oracle's
+restatement of the reference (windowing src/gpu_filter.cu:71-162 and
+src/batch_processor.cpp:100-266; filter src/gpu_filter.cu:183-309).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def expected_filtered(O, r2p, img, raw, prior=None):
+    raw8 = np.ascontiguousarray(raw).view(np.uint8).reshape(-1)
+    p = O.OrcParams.from_buffer_copy(bytes(img.dicom))
+    if img.window_mode == r2p.WINDOW_BATCH8:
+        win, _ = O.window8(raw8, p)
+    elif img.window_mode == r2p.WINDOW_DICOM16:
+        win = O.window_a2(raw8, p)
+    elif img.window_mode == r2p.WINDOW_SWAP16:
+        win = raw8.reshape(-1, 2)[:, ::-1].reshape(-1).copy()
+    else:
+        win = raw8
+    rb = img.row_bytes
+    bpp = img.channels * img.out_bytes_per_sample
+    return O.filter_rows(win, img.height, rb, bpp, prior), win
+
+
+def check(engine, O, r2p, img, raw, prior=None):
+    want, win = expected_filtered(O, r2p, img, raw, prior)
+    got = engine.filter_image(img, raw, prior)
+    if not np.array_equal(got, want):
+        rb = img.row_bytes + 1
+        bad = np.nonzero(got != want)[0]
+        r = bad[0] // rb
+        raise AssertionError("mismatch at byte %d (row %d col %d, type got %d want %d), %d bytes differ"
+                             % (bad[0], r, bad[0] % rb, got[r * rb], want[r * rb], bad.size))
+    return want
+
+
+def test_c0_q15(engine, O, r2p, W):
+    raw = W.ct_phantom(0)
+    img = W.image_c0()
+    p = O.OrcParams.from_buffer_copy(bytes(img.dicom))
+    assert O.q15_coeffs(p) is not None          # WW 400 takes the Q15 path
+    check(engine, O, r2p, img, raw)
+
+
+@pytest.mark.parametrize("ww", [150.0, 80.0, 254.0])
+def test_batch8_lut_narrow_window(engine, O, r2p, W, ww):
+    raw = W.ct_phantom(1, 300, 211)
+    img = W.image_ct8(300, 211, 60.0, ww)
+    assert O.q15_coeffs(O.OrcParams.from_buffer_copy(bytes(img.dicom))) is None   # table fallback
+    check(engine, O, r2p, img, raw)
+
+
+def test_batch8_shifted_and_signed(engine, O, r2p, W):
+    rng = np.random.default_rng(5)
+    raw = rng.integers(0, 65536, size=(97, 130), dtype=np.uint16).astype("<u2")
+    for hb, pr in ((15, 0), (11, 1), (15, 1)):
+        p = r2p.DicomParams.make(16, 12, hb, pr, slope=1.5, intercept=-300.0, wc=100.0, ww=900.0)
+        img = r2p.Image.make(130, 97, 1, 2, r2p.WINDOW_BATCH8, p)
+        check(engine, O, r2p, img, raw)
+
+
+def test_batch8_no_window(engine, O, r2p):
+    rng = np.random.default_rng(6)
+    raw = rng.integers(0, 4096, size=(64, 64), dtype=np.uint16).astype("<u2")
+    for pr in (0, 1):
+        p = r2p.DicomParams.make(16, 12, 11, pr)
+        img = r2p.Image.make(64, 64, 1, 2, r2p.WINDOW_BATCH8, p)
+        check(engine, O, r2p, img, raw)
+
+
+def test_dicom16_lut(engine, O, r2p, W):
+    raw = W.radial_rects(1, 320, 200)
+    img = r2p.Image.make(320, 200, 1, 2, r2p.WINDOW_DICOM16, r2p.DicomParams.make(16, 12, 11, 0, wc=2048.0, ww=4096.0))
+    check(engine, O, r2p, img, raw)
+
+
+def test_dicom16_direct_signed_rescale(engine, O, r2p):
+    rng = np.random.default_rng(7)
+    raw = rng.integers(0, 65536, size=(50, 77), dtype=np.uint16).astype("<u2")
+    p = r2p.DicomParams.make(16, 16, 15, 1, slope=0.7, intercept=-100.0, wc=30.0, ww=2500.0)
+    img = r2p.Image.make(77, 50, 1, 2, r2p.WINDOW_DICOM16, p)
+    check(engine, O, r2p, img, raw)
+    p = r2p.DicomParams.make(16, 14, 15, 0, slope=2.0, wc=900.0, ww=0.5)   # step function (w-1 <= 0)
+    img = r2p.Image.make(77, 50, 1, 2, r2p.WINDOW_DICOM16, p)
+    check(engine, O, r2p, img, raw)
+
+
+def test_dicom16_8bit_input(engine, O, r2p):
+    rng = np.random.default_rng(8)
+    raw = rng.integers(0, 256, size=(40, 99), dtype=np.uint8)
+    p = r2p.DicomParams.make(8, 8, 7, 1, slope=1.0, intercept=5.0, wc=10.0, ww=120.0)
+    img = r2p.Image.make(99, 40, 1, 1, r2p.WINDOW_DICOM16, p)
+    check(engine, O, r2p, img, raw)
+
+
+def test_rgb16_unaligned_rows(engine, O, r2p, W):
+    raw = W.rgb_sinusoids(2, 257, 33)
+    img = r2p.Image.make(257, 33, 3, 2, r2p.WINDOW_NONE)
+    check(engine, O, r2p, img, raw)
+
+
+def test_rgb16_c2_shape_rows(engine, O, r2p, W):
+    raw = W.rgb_sinusoids(3, 6000, 24)
+    img = r2p.Image.make(6000, 24, 3, 2, r2p.WINDOW_NONE)
+    check(engine, O, r2p, img, raw)
+
+
+def test_rgba8_and_swap16(engine, O, r2p):
+    rng = np.random.default_rng(9)
+    raw = rng.integers(0, 256, size=(31, 45, 4), dtype=np.uint8)
+    check(engine, O, r2p, r2p.Image.make(45, 31, 4, 1, r2p.WINDOW_NONE), raw)
+    raw16 = rng.integers(0, 65536, size=(29, 51), dtype=np.uint16).astype("<u2")
+    check(engine, O, r2p, r2p.Image.make(51, 29, 1, 2, r2p.WINDOW_SWAP16), raw16)
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (1, 7), (2, 3), (3, 1), (5, 9), (17, 4), (4097, 3), (8193, 2)])
+def test_ragged_sizes(engine, O, r2p, w, h):
+    rng = np.random.default_rng(w * 31 + h)
+    raw = rng.integers(0, 256, size=(h, w), dtype=np.uint8)
+    check(engine, O, r2p, r2p.Image.make(w, h, 1, 1, r2p.WINDOW_NONE), raw)
+
+
+def test_widest_row(engine, O, r2p):
+    # 17043-pixel RGB16 rows, the widest image the reference describes
+    rng = np.random.default_rng(10)
+    raw = rng.integers(0, 65536, size=(3, 17043, 3), dtype=np.uint16).astype(">u2")
+    check(engine, O, r2p, r2p.Image.make(17043, 3, 3, 2, r2p.WINDOW_NONE), raw)
+
+
+def test_prior_row(engine, O, r2p):
+    # strip semantics: the caller's windowed row above row 0
+    rng = np.random.default_rng(11)
+    raw = rng.integers(0, 256, size=(9, 300), dtype=np.uint8)
+    prior = rng.integers(0, 256, size=300, dtype=np.uint8)
+    check(engine, O, r2p, r2p.Image.make(300, 9, 1, 1, r2p.WINDOW_NONE), raw, prior)
+
+
+def test_all_filter_types_chosen(engine, O, r2p, W):
+    # a mixed image whose rows pick every one of the five filters
+    raw = W.rgb_sinusoids(4, 640, 64)
+    img = r2p.Image.make(640, 64, 3, 2, r2p.WINDOW_NONE)
+    want = check(engine, O, r2p, img, raw)
+    rng = np.random.default_rng(12)
+    noise = rng.integers(0, 256, size=(64, 640), dtype=np.uint8)
+    noise[::4] = 7
+    want2 = check(engine, O, r2p, r2p.Image.make(640, 64, 1, 1, r2p.WINDOW_NONE), noise)
+    types = set(want[::img.row_bytes + 1]) | set(want2[::641])
+    assert len(types) >= 3
+
+
+def test_random_fuzz(engine, O, r2p):
+    rng = np.random.default_rng(13)
+    for _ in range(12):
+        w = int(rng.integers(1, 900))
+        h = int(rng.integers(1, 60))
+        mode = int(rng.integers(0, 4))
+        if mode == r2p.WINDOW_BATCH8:
+            p = r2p.DicomParams.make(16, 12, 11, int(rng.integers(0, 2)), slope=1.0, intercept=-1024.0,
+                                     wc=float(rng.uniform(-600, 400)), ww=float(rng.uniform(80, 1600)))
+            img = r2p.Image.make(w, h, 1, 2, mode, p)
+            raw = rng.integers(0, 4096, size=(h, w), dtype=np.uint16).astype("<u2")
+        elif mode == r2p.WINDOW_DICOM16:
+            p = r2p.DicomParams.make(16, 12, 11, 0, wc=float(rng.uniform(0, 4096)), ww=float(rng.uniform(2, 4096)))
+            img = r2p.Image.make(w, h, 1, 2, mode, p)
+            raw = rng.integers(0, 4096, size=(h, w), dtype=np.uint16).astype("<u2")
+        else:
+            ch = int(rng.choice([1, 3, 4]))
+            bps = int(rng.integers(1, 3)) if mode == r2p.WINDOW_NONE else 2
+            img = r2p.Image.make(w, h, ch, bps, mode)
+            raw = rng.integers(0, 256, size=w * h * ch * bps, dtype=np.uint8)
+        check(engine, O, r2p, img, raw)

@@ -1,0 +1,114 @@
+"""The oracle, pinned against golden vectors from the reference's own code.
+
+tests/golden/window8_ref.npz holds outputs of the reference's own 16->8-bit
+windowing functions (src/batch_processor.cpp:100-266, dispatch :397-409);
+tests/golden/cpu_png_ref.json holds sha256/size of PNGs written by the
+reference's own deflate_strip + PngWriter.  Both were produced by
+tests/golden/gen_golden.py from the reference sources.
+"""
+import hashlib
+import json
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def params_from_row(O, row):
+    p = O.OrcParams()
+    (p.bits_allocated, p.bits_stored, p.high_bit, p.pixel_rep, p.apply_rescale) = [int(v) for v in row[:5]]
+    p.rescale_slope, p.rescale_intercept = float(row[5]), float(row[6])
+    p.apply_window = int(row[7])
+    p.window_center, p.window_width = float(row[8]), float(row[9])
+    return p
+
+
+def test_window8_matches_reference_vectors(O):
+    g = np.load(os.path.join(GOLDEN, "window8_ref.npz"))
+    raw = g["raw"].view(np.uint8)
+    n_q15 = n_lut = 0
+    for row, out, path in zip(g["params"], g["out"], g["path"]):
+        p = params_from_row(O, row)
+        got, gp = O.window8(raw, p)
+        assert gp == path
+        assert np.array_equal(got, out)
+        n_q15 += gp == 1
+        n_lut += gp == 2
+    assert n_q15 > 5 and n_lut > 5          # both reference paths are covered
+
+
+def test_c0_phantom_window_matches_reference(O, W):
+    g = np.load(os.path.join(GOLDEN, "window8_ref.npz"))
+    raw = W.ct_phantom(0)
+    assert np.array_equal(raw, g["c0_raw"])   # the generator is stable
+    got, path = O.window8(raw.view(np.uint8), O.make_params(16, 12, 11, 0, slope=1.0, intercept=-1024.0,
+                                                           wc=40.0, ww=400.0))
+    assert path == int(g["c0_path"]) == 1
+    assert np.array_equal(got, g["c0_out"])
+
+
+def test_q15_and_lut_disagree_by_one(O):
+    # the two reference CPU paths differ by 1 LSB on ordinary CT values, so the
+    # dispatch must be reproduced exactly (probe values 0x428, 0, 0xFFF, 0x450)
+    p = O.make_params(16, 12, 11, 0, slope=1.0, intercept=-1024.0, wc=40.0, ww=400.0)
+    v = np.array([0x428, 0, 0xFFF, 0x450], "<u2").view(np.uint8)
+    q, path = O.window8(v, p)
+    assert path == 1 and list(q) == [127, 0, 255, 152]
+    lut = O.build_lut(p)
+    assert [int(lut[x]) for x in (0x428, 0, 0xFFF, 0x450)] == [128, 0, 255, 153]
+
+
+def test_port_png_matches_reference_bytes(O, W):
+    with open(os.path.join(GOLDEN, "cpu_png_ref.json")) as f:
+        ref = json.load(f)
+    if zlib.ZLIB_RUNTIME_VERSION != ref["zlib"]:
+        pytest.skip("PNG bytes are pinned for zlib %s" % ref["zlib"])
+    c0 = W.ct_phantom(0)
+    c0_out, _ = O.window8(c0.view(np.uint8), O.make_params(16, 12, 11, 0, slope=1.0, intercept=-1024.0,
+                                                          wc=40.0, ww=400.0))
+    filt_c0 = O.filter_rows(c0_out, 512, 512, 1)
+    rng = np.random.default_rng(5)
+    small = (rng.integers(0, 40, size=200 * 333) + np.arange(200 * 333) // 97 % 7).astype(np.uint8)
+    filt_small = O.filter_rows(small, 200, 333, 1)
+    inputs = {"c0": (filt_c0, 512, 512), "small": (filt_small, 333, 200)}
+    for case in ref["cases"]:
+        filt, w, h = inputs[case["name"].split("_")[0]]
+        enc = O.PortEncoder(case["threads"])
+        png = enc.png_from_filtered(filt, w, h, w, 8, 1, case["level"], case["strip_height"])
+        enc.close()
+        assert len(png) == case["size"]
+        assert hashlib.sha256(png).hexdigest() == case["sha256"]
+
+
+def test_filter_known_answer(O):
+    # 2 rows x 4 bytes, bpp 1, worked by hand from the PNG filter definitions
+    img = np.array([[10, 20, 30, 40], [12, 22, 29, 41]], np.uint8)
+    out = O.filter_rows(img, 2, 4, 1).reshape(2, 5)
+    # row 0 (row above = zeros): Sub gives 10,10,10,10 (score 40) < None 100,
+    # Up 100, Avg 10,15,20,25 = 70, Paeth = Sub here -> ties go to the lower type
+    assert list(out[0]) == [1, 10, 10, 10, 10]
+    # row 1: Up gives 2,2,255,1 -> costs 2+2+1+1 = 6, the minimum
+    assert list(out[1]) == [2, 2, 2, 255, 1]
+
+
+def test_filter_unfilter_round_trip(O):
+    rng = np.random.default_rng(3)
+    for (h, rb, bpp) in ((5, 12, 3), (17, 101, 1), (3, 48, 6), (1, 1, 1), (9, 64, 8)):
+        img = rng.integers(0, 256, size=h * rb, dtype=np.uint8)
+        filt = O.filter_rows(img, h, rb, bpp)
+        assert np.array_equal(O.unfilter(filt, h, rb, bpp), img)
+
+
+def test_parse_png_rejects_bad_crc(O, W):
+    enc = O.PortEncoder(2)
+    raw = W.ct_phantom(1, 64, 32)
+    png = bytearray(enc.encode(raw.view(np.uint8), 64, 32, 1, 2, 2,
+                               O.make_params(16, 12, 11, 0, wc=40.0, ww=400.0), 1, 16))
+    enc.close()
+    O.parse_png(bytes(png))
+    png[40] ^= 1
+    with pytest.raises(ValueError):
+        O.parse_png(bytes(png))
