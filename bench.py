@@ -1,0 +1,365 @@
+"""Benchmark: raw-pixel MB/s and images/s of the GB300 PNG encoder.
+
+A step is one pass of the encode path over one image of the workload.  The
+default workload is a single 3072x3072 uint16 image (12 bits stored, DICOM
+PS3.3 window WC 2048 / WW 4096 to 16-bit output, adaptive filter, LZ77 +
+fixed Huffman at level 1 in 65520-byte blocks).  Eight distinct inputs are
+rotated so the working set (151 MB of raw pixels) exceeds the 129 MB L2.
+
+  value     device-resident throughput: pixels and PNG in HBM, timed with CUDA
+            events on the encode stream, max over ranks
+  e2e       the same metric through r2p_encode_png with pinned host buffers:
+            host->device pixels and device->host PNG inside the timed region
+  roofline  dominant kernel: algorithmic bytes per launch / its mean duration
+            (CUDA events around each stage inside the timed region)
+  cpu_baseline  the oracle's CPU restatement of the reference path (window,
+            filter, strip-parallel zlib level 1, PNG container) on this host
+
+`--impl reference` times that CPU path alone (all host threads) on the same
+workload and metric.  Multi-GPU runs (torchrun) are independent replicas:
+each rank encodes its own images, no collective on the data path.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "raw-pixel MB/s"
+UNIT = "MB/s"
+
+
+def workload_desc(name):
+    return {
+        "c1": "single 3072x3072 uint16 image (12 bits stored), DICOM window WC 2048/WW 4096 to 16-bit, "
+              "adaptive filter, LZ77 + fixed Huffman level 1, 65520-byte independent blocks",
+        "c0": "single 512x512 uint16 CT phantom (12 bits stored), slope 1 / intercept -1024, WC 40/WW 400 to "
+              "8-bit (Q15 path), adaptive filter, stored DEFLATE (level 0)",
+        "c2": "single 6000x4000 RGB uint16 image, no window, adaptive filter, LZ77 + fixed Huffman level 1",
+    }[name]
+
+
+def make_inputs(W, name, nvar):
+    if name == "c1":
+        base = W.radial_rects(1, 3072, 3072)
+        img = W.image_c1(level=1)
+    elif name == "c0":
+        base = W.ct_phantom(0)
+        img = W.image_c0()
+    else:
+        base = W.rgb_sinusoids(2, 6000, 4000)
+        img = W.image_c2(level=1)
+    raws = [np.ascontiguousarray(np.roll(base, 97 * k, axis=1)) for k in range(nvar)]
+    return img, raws
+
+
+def cpu_params(O, img):
+    return O.OrcParams.from_buffer_copy(bytes(img.dicom))
+
+
+def window_mode_for_port(r2p, img):
+    return {r2p.WINDOW_NONE: 0, r2p.WINDOW_DICOM16: 1, r2p.WINDOW_BATCH8: 2}[img.window_mode]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*%s\s+%s\s*=\s*([0-9]+)" % (re.escape(kernel), re.escape(workload)),
+                  text)
+    return int(m.group(1)) if m else None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return 0, 1, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(O, r2p, img, raws, seconds=2.0, min_images=2):
+    threads = os.cpu_count() or 1
+    enc = O.PortEncoder(threads)
+    mode = window_mode_for_port(r2p, img)
+    p = cpu_params(O, img)
+    strip = 256
+    enc.encode(raws[0].view(np.uint8), img.width, img.height, img.channels, img.bytes_per_sample, mode, p,
+               img.level, strip)   # warm the pool
+    n, t0 = 0, time.perf_counter()
+    while n < min_images or time.perf_counter() - t0 < seconds:
+        enc.encode(raws[n % len(raws)].view(np.uint8), img.width, img.height, img.channels, img.bytes_per_sample,
+                   mode, p, img.level, strip)
+        n += 1
+    dt = time.perf_counter() - t0
+    enc.close()
+    return {"value": round(n * img.raw_bytes / dt / 1e6, 2), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d images of the workload (%.1f s wall), strip height %d, zlib level %d, %d threads"
+                      % (n, dt, strip, img.level, threads),
+            "images_per_s": round(n / dt, 3)}
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_setup()
+    if rank != 0:
+        return
+    import __graft_entry__ as g
+    r2p = g.load_package()
+    from raw2png_gb300 import workloads as W
+    from oracle import build_oracle, oracle as O
+    build_oracle.build_oracle()
+    img, raws = make_inputs(W, args.workload, 2)
+    threads = os.cpu_count() or 1
+    enc = O.PortEncoder(threads)
+    mode = window_mode_for_port(r2p, img)
+    p = cpu_params(O, img)
+    row = img.width * img.channels * img.bytes_per_sample
+
+    def enc_rows(k, rows):
+        src = raws[k % 2].view(np.uint8).reshape(img.height, row)[:rows]
+        enc.encode(src, img.width, rows, img.channels, img.bytes_per_sample, mode, p, img.level, 256)
+
+    # a step is the whole image, or a band of its top rows when K whole images
+    # would not finish within about 90 s on this host
+    t0 = time.perf_counter()
+    enc_rows(0, img.height)
+    t_img = time.perf_counter() - t0
+    rows = img.height
+    if args.steps * t_img > 90.0:
+        rows = max(64, min(img.height, int(img.height * 90.0 / (args.steps * t_img))))
+    for i in range(args.warmup):
+        enc_rows(i, rows)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        enc_rows(i, rows)
+    dt = time.perf_counter() - t0
+    enc.close()
+    step_bytes = rows * row
+    v = round(args.steps * step_bytes / dt / 1e6, 2)
+    sample = ("%d steps of %d of the image's %d rows (%.1f MB raw each), strip height 256, zlib level %d, "
+              "%d threads: CPU restatement of the reference's window/filter + its zlib strip pipeline"
+              % (args.steps, rows, img.height, step_bytes / 1e6, img.level, threads))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic", "config": {"workload": workload_desc(args.workload), "images_per_step": 1,
+                                            "rows_per_step": rows},
+            "images_per_s": round(args.steps * rows / img.height / dt, 3),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, world, local, dist = dist_setup()
+    import __graft_entry__ as g
+    r2p = g.load_package()
+    from raw2png_gb300 import workloads as W
+    nvar = 8
+    img, raws = make_inputs(W, args.workload, nvar)
+    eng = r2p.Engine(local)
+    stream = r2p.Stream()
+    cap = r2p.png_bound(img)
+    d_raw = [r2p.DeviceBuffer.from_array(r) for r in raws]
+    d_png = [r2p.DeviceBuffer(cap) for _ in range(nvar)]
+    d_len = r2p.DeviceBuffer(8 * nvar)
+    ev0, ev1 = r2p.Event(), r2p.Event()
+
+    def step(i):
+        k = i % nvar
+        eng.encode_png_device(img, d_raw[k].ptr, d_png[k].ptr, cap, d_len.ptr + 8 * k, stream)
+
+    for i in range(args.warmup):
+        step(i)
+    stream.sync()
+    # timed region (device)
+    clocks = ClockSampler(local)
+    clocks.start()
+    eng.set_timing(True)
+    barrier(dist)
+    stream.sync()
+    launches0 = r2p.launch_count()
+    ev0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    ev1.record(stream)
+    stream.sync()
+    barrier(dist)
+    launches = r2p.launch_count() - launches0
+    ms = ev0.elapsed_ms(ev1)
+    stages = eng.stage_times()
+    eng.set_timing(False)
+    clk = clocks.stop()
+    ms_max = max_over_ranks(dist, ms)
+    total_bytes = img.raw_bytes * args.steps * world
+    value = total_bytes / (ms_max / 1e3) / 1e6
+    # output sanity (not timed): one PNG inflates to the right size
+    lens = d_len.download(8 * nvar).view(np.uint64)
+    png = d_png[0].download(int(lens[0])).tobytes()
+    import zlib
+    filt = zlib.decompress(png[41:len(png) - 16])      # IDAT data: zlib header .. Adler-32
+    assert len(filt) == img.filtered_bytes, "benchmarked PNG does not inflate to the filtered size"
+    comp_bytes = len(png)
+    # e2e through the host entry point with pinned buffers
+    pin_in = [r2p.PinnedBuffer(img.raw_bytes) for _ in range(2)]
+    for k in range(2):
+        pin_in[k].array[:] = raws[k].view(np.uint8).reshape(-1)
+    pin_out = r2p.PinnedBuffer(cap)
+    import ctypes
+    n = ctypes.c_size_t()
+    L = r2p.lib()
+
+    def e2e_step(i):
+        r2p.check(L.r2p_encode_png(eng.h, ctypes.byref(img), pin_in[i % 2].ptr, pin_out.ptr, cap, ctypes.byref(n)))
+
+    for i in range(max(2, args.warmup)):
+        e2e_step(i)
+    e2e_steps = args.steps
+    barrier(dist)
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        e2e_step(i)
+    t1 = time.perf_counter()
+    barrier(dist)
+    e2e_s = max_over_ranks(dist, t1 - t0)
+    e2e_value = img.raw_bytes * e2e_steps * world / e2e_s / 1e6
+    if rank != 0:
+        return
+    # roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    dom = max(stages.items(), key=lambda kv: kv[1][0])
+    dname, (dms, dl) = dom
+    per_launch_ms = dms / max(dl, 1)
+    stream_bytes = comp_bytes - 63
+    alg = {"window_filter": img.raw_bytes + img.filtered_bytes,
+           "lz77_blocks": img.filtered_bytes + stream_bytes,
+           "stored_blocks": img.filtered_bytes + stream_bytes,
+           "copy_blocks": 2 * stream_bytes,
+           "finalize": 0, "prepare_window": 0}[dname]
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    kname = r2p.KERNELS[r2p.STAGES.index(dname)]
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": workload_desc(args.workload), "images_per_step": 1,
+                   "l2": "%d distinct inputs rotated (%.0f MB raw > 129 MB L2)" % (nvar, nvar * img.raw_bytes / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "images_per_s": round(args.steps * world / (ms_max / 1e3), 2),
+        "png_bytes": comp_bytes,
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": img.raw_bytes,
+                "d2h_bytes_per_step": comp_bytes + 8,
+                "images_per_s": round(e2e_steps * world / e2e_s, 2)},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": round(per_launch_ms, 5),
+                     "traffic": ncu_traffic(kname, args.workload)},
+        "stages_ms_per_step": {k: round(v[0] / max(v[1], 1), 5) for k, v in stages.items() if v[1]},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        from oracle import build_oracle, oracle as O
+        build_oracle.build_oracle()
+        line["cpu_baseline"] = cpu_baseline(O, r2p, img, raws)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -156,6 +156,19 @@ int  r2p_event_create(void** ev);
 int  r2p_event_destroy(void* ev);
 int  r2p_event_record(void* ev, void* stream);
 int  r2p_event_elapsed_ms(void* ev_start, void* ev_end, float* ms);
+/* Stage timing: when enabled, each encode call records CUDA events on its
+ * stream between its kernel launches; r2p_engine_stage_times() waits for
+ * them, returns per-stage device milliseconds summed over the calls since the
+ * last query (and how many launches each sum covers), and resets. */
+#define R2P_STAGE_PREPARE  0   /* k_prepare_window: window tables */
+#define R2P_STAGE_FILTER   1   /* k_window_filter: window + adaptive filter */
+#define R2P_STAGE_STORED   2   /* k_stored_blocks: level-0 DEFLATE */
+#define R2P_STAGE_LZ77     3   /* k_lz77_blocks: LZ77 + fixed Huffman */
+#define R2P_STAGE_FINALIZE 4   /* k_finalize: checksums + PNG chunks */
+#define R2P_STAGE_COPY     5   /* k_copy_blocks: block gather */
+#define R2P_STAGE_COUNT    6
+int r2p_engine_set_timing(r2p_engine* eng, int enable);
+int r2p_engine_stage_times(r2p_engine* eng, double* ms, uint64_t* launches);
 /* Kernels this library launched since the process started (all streams). */
 uint64_t r2p_kernel_launch_count(void);
 

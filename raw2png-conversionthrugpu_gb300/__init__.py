@@ -147,7 +147,12 @@ SIGNATURES = {
     "r2p_event_record": (ctypes.c_int, [_vp, _vp]),
     "r2p_event_elapsed_ms": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(ctypes.c_float)]),
     "r2p_kernel_launch_count": (ctypes.c_uint64, []),
+    "r2p_engine_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "r2p_engine_stage_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _u64p]),
 }
+
+STAGES = ["prepare_window", "window_filter", "stored_blocks", "lz77_blocks", "finalize", "copy_blocks"]
+KERNELS = ["k_prepare_window", "k_window_filter", "k_stored_blocks", "k_lz77_blocks", "k_finalize", "k_copy_blocks"]
 
 
 def lib():
@@ -358,6 +363,16 @@ class Engine:
 
     def crc32_device(self, d_data, n, d_result, stream=None):
         check(lib().r2p_crc32_device(self.h, d_data, n, d_result, _sp(stream)))
+
+    def set_timing(self, enable=True):
+        check(lib().r2p_engine_set_timing(self.h, 1 if enable else 0))
+
+    def stage_times(self):
+        """{stage: (total ms, launches)} since the last query."""
+        ms = (ctypes.c_double * len(STAGES))()
+        n = (ctypes.c_uint64 * len(STAGES))()
+        check(lib().r2p_engine_stage_times(self.h, ms, n))
+        return {STAGES[i]: (ms[i], int(n[i])) for i in range(len(STAGES))}
 
     # convenience wrappers that move data through host memory (tests)
     def filter_image(self, img, pixels, prior=None):

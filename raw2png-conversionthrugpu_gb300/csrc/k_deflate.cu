@@ -210,7 +210,7 @@ k_copy_blocks(const DevImage* __restrict__ imgs, const BlockOut* __restrict__ bl
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
         const BlockOut& bo = blocks[b];
         const DevImage& d = imgs[bo.img];
-        if (d.status) continue;
+        if (d.status || d.level == 0) continue;   // stored blocks are already in place
         cta_copy_to_global<kCopyThreads>(d.png + d.prefix + bo.out_off, scratch + (size_t)b * slot_bytes,
                                          (int)bo.out_len);
     }

@@ -183,6 +183,11 @@ struct r2p_engine {
     cudaEvent_t staged = nullptr;   // descriptor upload of the previous call
     bool have_done = false;
     std::mutex mu;
+    // stage timing (events between stage launches on the call's stream)
+    bool timing = false;
+    std::vector<std::vector<cudaEvent_t>> trec;   // per timed call: R2P_STAGE_COUNT + 1 events
+    std::vector<uint32_t> tmask;                  // stages each timed call launched
+    size_t tused = 0;
 };
 
 namespace r2p {
@@ -337,22 +342,46 @@ static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers&
     DevImage* dimg = reinterpret_cast<DevImage*>(A + P.o_img);
     BandItem* ditems = reinterpret_cast<BandItem*>(A + P.o_items);
     BlockOut* dblocks = reinterpret_cast<BlockOut*>(A + P.o_blocks);
+    std::vector<cudaEvent_t>* tev = nullptr;
+    if (e->timing) {
+        if (e->tused == e->trec.size()) {
+            std::vector<cudaEvent_t> v(R2P_STAGE_COUNT + 1);
+            for (auto& ev : v) R2P_CU(cudaEventCreate(&ev), "cudaEventCreate");
+            e->trec.push_back(v);
+            e->tmask.push_back(0);
+        }
+        tev = &e->trec[e->tused];
+        e->tmask[e->tused] = 0;
+        e->tused++;
+    }
+    // event k marks the start of stage k; a skipped stage records an empty interval
+    auto mark = [&](int k, bool ran) -> cudaError_t {
+        if (!tev) return cudaSuccess;
+        if (ran) e->tmask[e->tused - 1] |= 1u << (k - 1);
+        return cudaEventRecord((*tev)[k], s);
+    };
+    R2P_CU(mark(0, false), "event");
+    if (stages & ST_FILTER) R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
+    R2P_CU(mark(1, (stages & ST_FILTER) != 0), "event");
     if (stages & ST_FILTER) {
-        R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
         const int grid = (int)std::min<size_t>(P.items.size(), (size_t)P.slots_total);
         R2P_CU(launch_window_filter(dimg, ditems, (int)P.items.size(), grid, P.smem, s), "k_window_filter");
     }
-    if (stages & ST_DEFLATE) {
-        const int grid = (int)std::min<uint64_t>(P.nblk, (uint64_t)e->nsm * 8);
-        if (P.any_stored)
-            R2P_CU(launch_stored(dimg, dblocks, (int)P.nblk, P.max_block, e->d_xpow, grid, s), "k_stored_blocks");
-        if (P.any_lz)
-            R2P_CU(launch_lz77(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, grid, s),
-                   "k_lz77_blocks");
-        R2P_CU(launch_finalize(dimg, n, dblocks, e->d_xpow, s), "k_finalize");
-        if (P.any_lz)
-            R2P_CU(launch_copy_blocks(dimg, dblocks, (int)P.nblk, A + P.o_scratch, P.slot, grid, s), "k_copy_blocks");
-    }
+    R2P_CU(mark(2, (stages & ST_FILTER) != 0), "event");
+    const bool defl = (stages & ST_DEFLATE) != 0;
+    const int bgrid = (int)std::min<uint64_t>(P.nblk, (uint64_t)e->nsm * 8);
+    if (defl && P.any_stored)
+        R2P_CU(launch_stored(dimg, dblocks, (int)P.nblk, P.max_block, e->d_xpow, bgrid, s), "k_stored_blocks");
+    R2P_CU(mark(3, defl && P.any_stored), "event");
+    if (defl && P.any_lz)
+        R2P_CU(launch_lz77(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, bgrid, s),
+               "k_lz77_blocks");
+    R2P_CU(mark(4, defl && P.any_lz), "event");
+    if (defl) R2P_CU(launch_finalize(dimg, n, dblocks, e->d_xpow, s), "k_finalize");
+    R2P_CU(mark(5, defl), "event");
+    if (defl && P.any_lz)
+        R2P_CU(launch_copy_blocks(dimg, dblocks, (int)P.nblk, A + P.o_scratch, P.slot, bgrid, s), "k_copy_blocks");
+    R2P_CU(mark(6, defl && P.any_lz), "event");
     R2P_CU(cudaEventRecord(e->done, s), "event");
     e->have_done = true;
     return R2P_OK;
@@ -437,6 +466,8 @@ void r2p_engine_destroy(r2p_engine* e)
     if (e->h_stage) cudaFreeHost(e->h_stage);
     if (e->done) cudaEventDestroy(e->done);
     if (e->staged) cudaEventDestroy(e->staged);
+    for (auto& v : e->trec)
+        for (auto ev : v) cudaEventDestroy(ev);
     delete e;
 }
 
@@ -636,6 +667,40 @@ int r2p_crc32_device(r2p_engine* e, const void* d_data, size_t len, uint32_t* d_
                            e->nsm * 4, s), "k_checksum");
     R2P_CU(cudaEventRecord(e->done, s), "event");
     e->have_done = true;
+    return R2P_OK;
+}
+
+int r2p_engine_set_timing(r2p_engine* e, int enable)
+{
+    if (!e) return set_err(R2P_EINVAL, "NULL engine");
+    std::lock_guard<std::mutex> lk(e->mu);
+    e->timing = enable != 0;
+    e->tused = 0;
+    return R2P_OK;
+}
+
+int r2p_engine_stage_times(r2p_engine* e, double* ms, uint64_t* launches)
+{
+    if (!e || !ms) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    for (int k = 0; k < R2P_STAGE_COUNT; k++) {
+        ms[k] = 0.0;
+        if (launches) launches[k] = 0;
+    }
+    for (size_t c = 0; c < e->tused; c++) {
+        auto& v = e->trec[c];
+        R2P_CU(cudaEventSynchronize(v[R2P_STAGE_COUNT]), "cudaEventSynchronize");
+        for (int k = 0; k < R2P_STAGE_COUNT; k++) {
+            if (!(e->tmask[c] & (1u << k))) continue;
+            float t = 0.f;
+            R2P_CU(cudaEventElapsedTime(&t, v[k], v[k + 1]), "cudaEventElapsedTime");
+            ms[k] += t;
+            if (launches) launches[k]++;
+        }
+    }
+    e->tused = 0;
     return R2P_OK;
 }
 
