@@ -130,6 +130,23 @@ int r2p_zlib_compress_device(r2p_engine* eng, const void* d_in, size_t len, int 
                              uint64_t* d_out_len, void* stream);
 size_t r2p_zlib_bound(size_t len, int level, int block_size);
 
+/* Allocation-free form of r2p_zlib_compress_device, for callers that cannot
+ * allocate device memory once running: code hosted in a framework that owns
+ * all GPU memory and forbids allocation after start-up, and latency-bound
+ * callers for which cudaMalloc/cudaFree would stall the device.  It has no
+ * counterpart in the reference.  It needs no engine: its scratch (work
+ * descriptors, per-block results, LZ77 block slots, CRC power table) lives in
+ * a 2 MiB static device array that every GPU loading the library holds until
+ * exit, so len is limited to 1 MiB (1048576 bytes); larger inputs are
+ * rejected with R2P_EINVAL.  The first call on a device sets the array up
+ * (looks up its address, builds the power table and waits for it): make that
+ * call before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU race: issue them on one stream or order them.  Output is
+ * byte-identical to r2p_zlib_compress_device for the same input, level and
+ * block_size. */
+int r2p_zlib_compress_noalloc(const void* d_in, size_t len, int level, int block_size,
+                              void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream);
+
 /* ---- checksums (device data) ------------------------------------------- */
 /* Replace gpu_adler32_compute (include/gpu_adler32.h:25) and
  * gpu_crc32_compute (include/gpu_crc32.h:29); results land in *d_result (a

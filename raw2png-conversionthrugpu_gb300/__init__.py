@@ -129,6 +129,7 @@ SIGNATURES = {
     "r2p_window_filter_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp]),
     "r2p_zlib_compress_device": (ctypes.c_int, [_vp, _vp, _sz, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _vp]),
     "r2p_zlib_bound": (_sz, [_sz, ctypes.c_int, ctypes.c_int]),
+    "r2p_zlib_compress_noalloc": (ctypes.c_int, [_vp, _sz, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _vp]),
     "r2p_adler32_device": (ctypes.c_int, [_vp, _vp, _sz, _vp, _vp]),
     "r2p_crc32_device": (ctypes.c_int, [_vp, _vp, _sz, _vp, _vp]),
     "r2p_crc32_combine": (ctypes.c_uint32, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64]),

@@ -403,6 +403,9 @@ static int bind(r2p_engine* e)
 
 }  // namespace r2p
 
+// status message hook for the other translation units of the library
+int r2p_internal_set_error(int code, const char* msg) { return r2p::set_err(code, msg); }
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
