@@ -101,7 +101,9 @@ int r2p_encode_png(r2p_engine* eng, const r2p_image* img, const void* h_pixels,
                    void* h_png, size_t png_cap, size_t* png_len);
 
 /* Device-resident form: pixels and PNG stay in HBM; the PNG size is written
- * to *d_png_len (a device uint64) when the work on `stream` completes.
+ * to *d_png_len (a device uint64) when the work on `stream` completes.  A
+ * device-side failure writes (1 << 63) | status there instead (R2P_ENOSPC,
+ * or R2P_ETIMEOUT when a bounded wait in a kernel gave up).
  * Replaces the modern path's filter -> gpu_deflate -> gpu_adler32 ->
  * gpu_png_assemble sequence (src/pipeline.cpp:581-830). */
 int r2p_encode_png_device(r2p_engine* eng, const r2p_image* img, const void* d_pixels,

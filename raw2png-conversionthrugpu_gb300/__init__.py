@@ -391,8 +391,8 @@ class Engine:
         ln = DeviceBuffer(8)
         self.zlib_compress_device(src.ptr, data.size, level, dst.ptr, cap, ln.ptr, block_size)
         n = int(ln.download(8).view(np.uint64)[0])
-        if n == 2 ** 64 - 1:
-            raise R2PError(ENOSPC, "zlib output overflow")
+        if n >> 63:
+            raise R2PError(n & 0xFF, "device reported an error")
         return dst.download(n).tobytes()
 
     def checksum(self, data, kind):

@@ -157,9 +157,9 @@ k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uin
     if (threadIdx.x == 0) {
         const bool png = (d.out_kind == 0);
         const uint64_t total = png ? (uint64_t)kPngPrefix + Ls + kPngSuffix : 2 + Ls + 4;
-        if (total > d.png_cap) {
-            d.status = R2P_ENOSPC;
-            *d.png_len = ~0ull;
+        if (d.status == 0 && total > d.png_cap) d.status = R2P_ENOSPC;
+        if (d.status) {                    // error word: top bit set, status in the low bits
+            *d.png_len = (1ull << 63) | (uint64_t)d.status;
             return;
         }
         const uint32_t adler = adler_from_sums(s1, s2 % kAdlerMod, F);

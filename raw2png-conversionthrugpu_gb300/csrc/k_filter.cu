@@ -23,6 +23,7 @@
 #include "r2p_common.h"
 #include "r2p_device.h"
 #include "r2p_kernels.h"
+#include "r2p_tma.cuh"
 
 namespace r2p {
 
@@ -248,6 +249,21 @@ __host__ __device__ inline int slot_stride(int rb)
     return 16 + ((rb + 15) & ~15) + 16;
 }
 
+// Raw bytes staged per row by the bulk-copy path (0 when rows are not
+// 16-byte multiples and the plain-load path is used).
+__host__ __device__ inline int staged_pitch(int in_pitch) { return (in_pitch & 15) ? 0 : in_pitch; }
+
+// Rows per tile for a given dynamic shared-memory size: the most rows, up to
+// two passes of the warp groups, whose staging + (rows+1) slots fit.
+__host__ __device__ inline int tile_rows_for(int rb, int in_pitch, int smem, int lreg, int cap_rows)
+{
+    const int stride = slot_stride(rb);
+    const int sp = staged_pitch(in_pitch);
+    for (int t = cap_rows; t >= 1; t--)
+        if (lreg + t * sp + (t + 1) * stride <= smem) return t;
+    return 0;
+}
+
 __host__ __device__ inline int lut_region_bytes(int mode, int entries, int esize)
 {
     const bool lut = (mode == W_A2_LUT) || (mode == W_LUT8);
@@ -405,26 +421,83 @@ __device__ __forceinline__ uint8_t filtered_byte(const uint8_t* xr, const uint8_
     return (uint8_t)filter_word(f, x, a, b, c);
 }
 
+// Window n staged raw rows (16-byte multiples, in shared memory) into their
+// ring slots.  All threads; no division: rows outer, 16-byte units inner.
+__device__ void window_staged_rows(const DevImage& d, const WinCtx& w, const uint8_t* stage, int n,
+                                   uint8_t* ring, int stride, int slots, int rel0, int tid, int nthr)
+{
+    const int units = d.in_pitch >> 4;
+    for (int j = 0; j < n; j++) {
+        const uint4* s4 = reinterpret_cast<const uint4*>(stage + (size_t)j * d.in_pitch);
+        uint8_t* dst = ring + ((rel0 + j) % slots) * stride + 16;
+        if (w.mode == W_COPY) {
+            for (int u = tid; u < units; u += nthr) reinterpret_cast<uint4*>(dst)[u] = s4[u];
+        } else if (w.ob == w.ib) {
+            for (int u = tid; u < units; u += nthr) {
+                const uint4 v = s4[u];
+                const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+                uint32_t o[4];
+                if (w.ib == 2) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        o[k] = winN(w, wv[k] & 0xFFFF) | (winN(w, wv[k] >> 16) << 16);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        uint32_t acc = 0;
+#pragma unroll
+                        for (int q = 0; q < 4; q++) acc |= winN(w, (wv[k] >> (8 * q)) & 0xFF) << (8 * q);
+                        o[k] = acc;
+                    }
+                }
+                reinterpret_cast<uint4*>(dst)[u] = make_uint4(o[0], o[1], o[2], o[3]);
+            }
+        } else {
+            for (int u = tid; u < units; u += nthr) {
+                const uint4 v = s4[u];
+                const uint32_t o0 = win8(w, v.x & 0xFFFF) | (win8(w, v.x >> 16) << 8) |
+                                    (win8(w, v.y & 0xFFFF) << 16) | (win8(w, v.y >> 16) << 24);
+                const uint32_t o1 = win8(w, v.z & 0xFFFF) | (win8(w, v.z >> 16) << 8) |
+                                    (win8(w, v.w & 0xFFFF) << 16) | (win8(w, v.w >> 16) << 24);
+                reinterpret_cast<uint2*>(dst)[u] = make_uint2(o0, o1);
+            }
+        }
+        const int tail0 = d.rb, tail1 = ((d.rb + 15) & ~15) + 16;
+        for (int i = tail0 + tid; i < tail1; i += nthr) dst[i] = 0;
+    }
+}
+
+// Time limit for one bulk copy of a tile to land in shared memory.
+constexpr uint64_t kBulkWaitNs = 200ull * 1000 * 1000;
+
 __global__ void __launch_bounds__(kFiltThreads)
-k_window_filter(const DevImage* __restrict__ imgs, const BandItem* __restrict__ items, int nitems,
-                int smem_bytes)
+k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items, int nitems, int smem_bytes)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint32_t red[kFiltWarps][5];
+    __shared__ __align__(8) uint64_t bar;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    uint32_t phase = 0;
 
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const BandItem bi = items[it];
-        const DevImage& d = imgs[bi.img];
+        DevImage& d = imgs[bi.img];
         const int rb = d.rb, bpp = d.bpp;
         const int lreg = lut_region_bytes(d.mode, d.lut_entries, d.lut_esize);
         const int stride = slot_stride(rb);
         const int G = warps_per_row(rb);
         const int rpp = kFiltWarps / G;                     // rows per pass
-        int slots = (smem_bytes - lreg) / stride;
-        if (slots > 2 * rpp + 1) slots = 2 * rpp + 1;
-        const int T = slots - 1;                            // rows per tile
-        uint8_t* ring = smem + lreg;
+        const int T = tile_rows_for(rb, d.in_pitch, smem_bytes, lreg, 2 * rpp);
+        const int slots = T + 1;
+        const int sp = staged_pitch(d.in_pitch);
+        uint8_t* stage = smem + lreg;
+        uint8_t* ring = stage + (size_t)T * sp;
+        // bulk copies need a 16-byte aligned source; otherwise plain loads
+        const bool bulk = sp > 0 && ((reinterpret_cast<uintptr_t>(d.raw) & 15) == 0);
 
         WinCtx w;
         w.mode = d.mode; w.ib = d.ib; w.ob = d.ob; w.shift = d.lut_shift; w.mask = d.lut_mask;
@@ -432,12 +505,17 @@ k_window_filter(const DevImage* __restrict__ imgs, const BandItem* __restrict__ 
         w.lut = (lreg > 0) ? smem : d.lut;
 
         __syncthreads();   // previous item finished with shared memory
+        if (bulk && tid == 0) {                            // first tile's raw rows
+            const int n0 = min(T, (int)bi.r1 - (int)bi.r0);
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar, (uint32_t)(n0 * sp));
+            bulk_g2s(stage, d.raw + (size_t)bi.r0 * d.in_pitch, (uint32_t)(n0 * sp), &bar);
+        }
         if (lreg > 0) {
             const uint4* s = reinterpret_cast<const uint4*>(d.lut);
             uint4* t = reinterpret_cast<uint4*>(smem);
             for (int i = tid; i < lreg / 16; i += kFiltThreads) t[i] = s[i];
         }
-        // zero the front guard of every slot
         for (int i = tid; i < slots * 4; i += kFiltThreads)
             reinterpret_cast<uint32_t*>(ring + (i >> 2) * stride)[i & 3] = 0u;
         __syncthreads();
@@ -459,12 +537,35 @@ k_window_filter(const DevImage* __restrict__ imgs, const BandItem* __restrict__ 
         for (int t0 = (int)bi.r0; t0 < (int)bi.r1; t0 += T) {
             const int n = min(T, (int)bi.r1 - t0);
             const int rel0 = t0 - (int)bi.r0 + 1;            // rel of the tile's first row
-            // window the tile's rows: warps take rows round-robin
-            for (int j = warp; j < n; j += kFiltWarps) {
-                uint8_t* dst = ring + ((rel0 + j) % slots) * stride + 16;
-                window_row_range(d, w, t0 + j, dst, lane, 32, aligned);
+            if (bulk) {
+                const bool ok = mbar_wait_bounded(&bar, phase, kBulkWaitNs);
+                if (__syncthreads_or(!ok)) {
+                    // the copy did not land in time: report, give it one more
+                    // bounded wait, and leave this kernel
+                    if (tid == 0) {
+                        atomicExch(&d.status, R2P_ETIMEOUT);
+                        mbar_wait_bounded(&bar, phase, kBulkWaitNs);
+                    }
+                    __syncthreads();
+                    return;
+                }
+                phase ^= 1u;
+                window_staged_rows(d, w, stage, n, ring, stride, slots, rel0, tid, kFiltThreads);
+                __syncthreads();
+                const int t1 = t0 + n;
+                if (t1 < (int)bi.r1 && tid == 0) {           // prefetch the next tile during filtering
+                    const int n1 = min(T, (int)bi.r1 - t1);
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(&bar, (uint32_t)(n1 * sp));
+                    bulk_g2s(stage, d.raw + (size_t)t1 * d.in_pitch, (uint32_t)(n1 * sp), &bar);
+                }
+            } else {
+                for (int j = warp; j < n; j += kFiltWarps) {
+                    uint8_t* dst = ring + ((rel0 + j) % slots) * stride + 16;
+                    window_row_range(d, w, t0 + j, dst, lane, 32, aligned);
+                }
+                __syncthreads();
             }
-            __syncthreads();
 
             const int nwords = (rb + 3) >> 2;
             const int g = warp / G, wg = warp % G;
@@ -573,26 +674,29 @@ int filter_lut_region(int mode, int lut_entries, int lut_esize)
     return lut_region_bytes(mode, lut_entries, lut_esize);
 }
 
-// Dynamic shared memory wanted for an image: LUT region plus 2*rows_per_pass+1
-// row slots (fewer when rows are wide); -1 when not even two slots fit.
-int filter_smem_bytes(int rb, int mode, int lut_entries, int lut_esize)
+// Per-CTA shared memory aimed at two CTAs per SM; wider rows take more.
+constexpr int kFilterSmemTarget = 108 * 1024;
+
+// Dynamic shared memory wanted for an image: LUT region, the staged raw rows
+// of one tile and tile+1 row slots, with the most rows (up to two passes of
+// the warp groups) that fit the two-CTA target, else the cap; -1 if even one
+// row does not fit.
+int filter_smem_bytes(int rb, int in_pitch, int mode, int lut_entries, int lut_esize)
 {
     const int lreg = lut_region_bytes(mode, lut_entries, lut_esize);
     const int stride = slot_stride(rb);
+    const int sp = staged_pitch(in_pitch);
     const int rpp = kFiltWarps / warps_per_row(rb);
-    int slots = 2 * rpp + 1;
-    if (lreg + slots * stride > kFilterSmemCap) slots = (kFilterSmemCap - lreg) / stride;
-    if (slots < 2) return -1;
-    return lreg + slots * stride;
+    int t = tile_rows_for(rb, in_pitch, kFilterSmemTarget, lreg, 2 * rpp);
+    if (t == 0) t = tile_rows_for(rb, in_pitch, kFilterSmemCap, lreg, 2 * rpp);
+    if (t == 0) return -1;
+    return lreg + t * sp + (t + 1) * stride;
 }
 
-int filter_tile_rows(int rb, int smem, int lut_region)
+int filter_tile_rows(int rb, int in_pitch, int smem, int lut_region)
 {
-    const int stride = slot_stride(rb);
     const int rpp = kFiltWarps / warps_per_row(rb);
-    int slots = (smem - lut_region) / stride;
-    if (slots > 2 * rpp + 1) slots = 2 * rpp + 1;
-    return slots - 1;
+    return tile_rows_for(rb, in_pitch, smem, lut_region, 2 * rpp);
 }
 
 int filter_ctas_per_sm(int smem)
@@ -611,7 +715,7 @@ cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_window_filter(const DevImage* imgs, const BandItem* items, int nitems, int grid, int smem,
+cudaError_t launch_window_filter(DevImage* imgs, const BandItem* items, int nitems, int grid, int smem,
                                  cudaStream_t s)
 {
     cudaError_t e = cudaFuncSetAttribute(k_window_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,

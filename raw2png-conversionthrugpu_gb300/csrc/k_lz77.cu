@@ -8,20 +8,21 @@
 // Only inflate-equality is required of the compressed bytes.
 //
 // Design.  One CTA per DEFLATE block (<= 65520 filtered bytes, staged in
-// shared memory).  Its 16 warps each parse a 1/16 segment greedily with a
-// private shared-memory hash table (most recent position per 4-byte hash,
-// seeded from the 4 KB before the segment) and may reference any earlier byte
-// of the block within 32 KB.  A warp examines 32 positions per step: every
-// lane tests three candidates (distance 1, the same column one scanline up,
-// the hash head) with word compares, a ballot chains the earliest matches
-// through the window, and a match that reaches the per-lane limit is extended
-// cooperatively (32 bytes per ballot).  Code lengths are prefix-summed across
-// the warp and each lane ORs its code into the warp's bitstream.  The 16
-// bitstreams are stitched at their bit offsets behind the 3-bit block header;
-// an end-of-block code and an empty stored block byte-align the output, so
-// blocks are independent and join by plain concatenation.  A block whose
-// Huffman form would not be smaller is emitted as a stored block.  The CTA
-// also leaves the block's Adler-32 sums (input) and CRC-32 (output).
+// shared memory).  Every one of the CTA's 512 threads parses its own
+// 132-byte sub-range of the block sequentially -- a greedy LZ77 with three
+// candidates per position: distance 1 (a run), the same column one scanline
+// up, and the head of a 4-byte hash table shared by the 32 lanes of a warp
+// (seeded from the 4 KB before the warp's range).  Matches may reach any
+// earlier byte of the block within 32 KB but end inside the thread's
+// sub-range, and are extended by word compares.  Each thread packs its
+// fixed-Huffman codes LSB-first into a 64-bit register and spills whole words
+// to a private shared-memory buffer (an odd word stride keeps the 32 lanes on
+// distinct banks), so no atomics are needed while parsing.  A CTA-wide scan
+// of the per-thread bit counts places the 512 bitstreams behind the 3-bit
+// block header; an end-of-block code and an empty stored block byte-align the
+// output, so blocks are independent and join by plain concatenation.  A block
+// whose Huffman form would not be smaller is emitted as a stored block.  The
+// CTA also leaves the block's Adler-32 sums (input) and CRC-32 (output).
 #include <cuda_runtime.h>
 
 #include "k_deflate.cuh"
@@ -31,21 +32,27 @@ namespace r2p {
 
 constexpr int kLzWarps = 16;
 constexpr int kLzThreads = kLzWarps * 32;
-constexpr int kHashBits = 10;
+constexpr int kHashBits = 11;
 constexpr int kHashSize = 1 << kHashBits;
-constexpr int kPrefill = 4096;        // history bytes hashed before a segment
-constexpr int kLaneCap = 16;          // per-lane match length before cooperative extension
+constexpr int kPrefill = 4096;        // history bytes hashed before a warp's range
 constexpr int kMaxDist = 32768;
 constexpr int kMaxMatch = 258;
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 
-__host__ __device__ inline int lz_seg_bytes(int block_size) { return (block_size + kLzWarps - 1) / kLzWarps; }
-__host__ __device__ inline int lz_out_words(int block_size) { return (lz_seg_bytes(block_size) * 9 + 31) / 32 + 8; }
+// Bytes each thread parses: a multiple of 4 whose word count is odd, so the 32
+// lanes of a warp, reading at the same offset of their sub-ranges, hit 32
+// distinct shared-memory banks.  Output words per thread use an odd stride too.
+__host__ __device__ inline int lz_sub_bytes(int block_size)
+{
+    const int w = ((block_size + kLzThreads - 1) / kLzThreads + 3) >> 2;
+    return 4 * (w | 1);
+}
+__host__ __device__ inline int lz_lane_words(int block_size) { return ((lz_sub_bytes(block_size) * 9 + 31) / 32 + 2) | 1; }
 __host__ __device__ inline int lz_in_bytes(int block_size) { return ((block_size + 15) & ~15) + 64; }
 
 static int lz_smem_bytes(int block_size)
 {
-    return 4096 + lz_in_bytes(block_size) + kLzWarps * (lz_out_words(block_size) + kHashSize) * 4 + 256;
+    return 4096 + lz_in_bytes(block_size) + kLzThreads * lz_lane_words(block_size) * 4 + kLzWarps * kHashSize * 2 + 256;
 }
 
 uint64_t lz77_slot_bytes(int block_size) { return (uint64_t)((block_size + kStoredHdr + 64 + 255) & ~255); }
@@ -59,42 +66,6 @@ __device__ __forceinline__ uint32_t ld32u(const uint8_t* base, int p)
 }
 
 __device__ __forceinline__ uint32_t hash4(uint32_t v) { return (v * 2654435761u) >> (32 - kHashBits); }
-
-// Length of the match between positions c < p, up to maxl (<= kLaneCap
-// checked here with word compares); 0 if the first four bytes differ.
-__device__ __forceinline__ int match_len(const uint8_t* in, int c, int p, uint32_t wp, int maxl)
-{
-    uint32_t x = ld32u(in, c) ^ wp;
-    if (x) return 0;
-    int L = 4;
-#pragma unroll
-    for (int k = 4; k < kLaneCap; k += 4) {
-        x = ld32u(in, c + k) ^ ld32u(in, p + k);
-        if (x) { L = k + ((__ffs(x) - 1) >> 3); break; }
-        L = k + 4;
-    }
-    return L < maxl ? L : maxl;
-}
-
-// Cooperative extension of a match beyond L (warp-uniform arguments).
-__device__ __forceinline__ int extend_match(const uint8_t* in, int p, int c, int L, int maxl, int lane)
-{
-    while (L < maxl) {
-        const int k = L + lane;
-        const bool eq = (k < maxl) && in[c + k] == in[p + k];
-        const uint32_t ne = __ballot_sync(FULL, !eq);
-        if (ne) return L + __ffs(ne) - 1;
-        L += 32;
-    }
-    return maxl;
-}
-
-__device__ __forceinline__ uint32_t lane_range(int a, int b)   // bits [a, b), 0 <= a <= b <= 32
-{
-    const uint32_t hi = (b >= 32) ? FULL : ((1u << b) - 1u);
-    const uint32_t lo = (a >= 32) ? FULL : ((1u << a) - 1u);
-    return hi & ~lo;
-}
 
 // Fixed-Huffman code of a literal byte: reversed code and its length.
 __device__ __forceinline__ void lit_code(uint32_t b, uint32_t& v, int& n)
@@ -137,90 +108,65 @@ __device__ __forceinline__ void match_code(int len, int dist, uint32_t& v, int& 
     n = cl + lne + 5 + dne;
 }
 
-// Greedy parse of in[s0, s1) by one warp into bitstream `out` (zeroed words).
-// Returns the number of bits written.
-__device__ uint32_t parse_segment(const uint8_t* in, int n, int s0, int s1, int rb1, uint32_t* tab, uint32_t* out,
-                                  int lane)
+// Greedy parse of in[s, e) by one thread into the word buffer `ob`.
+// `tab` is the warp's shared hash table (latest position + 1 per hash).
+// Returns the number of bits written; the last partial word is stored too.
+__device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, uint16_t* tab, uint32_t* ob)
 {
-    const int pf0 = s0 > kPrefill ? s0 - kPrefill : 0;
-    for (int q0 = pf0; q0 < s0; q0 += 32) {
-        const int q = q0 + lane;
-        if (q < s0 && q + 4 <= n) atomicMax(&tab[hash4(ld32u(in, q))], (uint32_t)(q + 1));
-    }
-    __syncwarp();
-    uint32_t bp = 0;
-    int pos = s0;
-    while (pos < s1) {
-        const int p = pos + lane;
-        const int wlen = min(32, s1 - pos);
-        const bool can = (lane < wlen) && (p + 4 <= s1);
-        int bestL = 0, bestD = 0;
-        uint32_t h = 0;
-        if (can) {
+    const bool vert = rb1 > 1 && rb1 <= kMaxDist;
+    uint64_t acc = 0;
+    int nacc = 0, nw = 0;
+    uint32_t bits = 0;
+    int p = s;
+    while (p < e) {
+        int L = 0, D = 0;
+        if (p + 4 <= e) {
             const uint32_t w = ld32u(in, p);
-            h = hash4(w);
-            const int maxl = min(kMaxMatch, s1 - p);
-            if (p >= 1) {
-                const int L = match_len(in, p - 1, p, w, maxl);
-                if (L > bestL) { bestL = L; bestD = 1; }
+            const uint32_t h = hash4(w);
+            const int t = tab[h];
+            tab[h] = (uint16_t)(p + 1);
+            if (p > 0 && w == (uint32_t)in[p - 1] * 0x01010101u) {
+                D = 1;
+            } else if (vert && p >= rb1 && ld32u(in, p - rb1) == w) {
+                D = rb1;
+            } else if (t) {
+                const int dist = p - (t - 1);
+                if (dist > 0 && dist <= kMaxDist && ld32u(in, t - 1) == w) D = dist;
             }
-            if (rb1 > 1 && rb1 <= kMaxDist && p >= rb1) {
-                const int L = match_len(in, p - rb1, p, w, maxl);
-                if (L > bestL) { bestL = L; bestD = rb1; }
-            }
-            const uint32_t t = tab[h];
-            if (t) {
-                const int c = (int)t - 1;
-                const int dist = p - c;
-                if (dist > 1 && dist <= kMaxDist && dist != rb1) {
-                    const int L = match_len(in, c, p, w, maxl);
-                    if (L > bestL) { bestL = L; bestD = dist; }
+            if (D) {
+                // extend by words, then bytes, up to the sub-range end
+                const int maxl = min(kMaxMatch, e - p);
+                const int c = p - D;
+                L = 4;
+                bool more = true;
+                while (more && L + 4 <= maxl) {
+                    const uint32_t x = ld32u(in, c + L) ^ ld32u(in, p + L);
+                    if (x) { L += (__ffs(x) - 1) >> 3; more = false; }
+                    else L += 4;
                 }
+                while (more && L < maxl && in[c + L] == in[p + L]) L++;
             }
         }
-        const uint32_t mm = __ballot_sync(FULL, bestL >= 4);
-        // resolve the greedy chain of tokens through this window
-        uint32_t lits = 0, starts = 0;
-        int myL = bestL;
-        int t = 0;
-        while (t < wlen) {
-            const uint32_t cand = mm & ~lane_range(0, t);
-            if (!cand) { lits |= lane_range(t, wlen); t = wlen; break; }
-            const int j = __ffs(cand) - 1;
-            lits |= lane_range(t, j);
-            int L = __shfl_sync(FULL, bestL, j);
-            const int D = __shfl_sync(FULL, bestD, j);
-            const int pj = pos + j;
-            if (L >= kLaneCap) L = extend_match(in, pj, pj - D, L, min(kMaxMatch, s1 - pj), lane);
-            if (lane == j) myL = L;
-            starts |= 1u << j;
-            t = j + L;
+        uint32_t v;
+        int nb;
+        if (L >= 4) {
+            match_code(L, D, v, nb);
+            p += L;
+        } else {
+            lit_code(in[p], v, nb);
+            p += 1;
         }
-        // insert this window's examined positions that precede the next token
-        if (can && lane < t) atomicMax(&tab[h], (uint32_t)(p + 1));
-        // emit
-        uint32_t v = 0;
-        int nb = 0;
-        if (lits & (1u << lane)) lit_code(in[p], v, nb);
-        else if (starts & (1u << lane)) match_code(myL, bestD, v, nb);
-        int incl = nb;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += y;
+        acc |= (uint64_t)v << nacc;
+        nacc += nb;
+        bits += (uint32_t)nb;
+        if (nacc >= 32) {
+            ob[nw++] = (uint32_t)acc;
+            acc >>= 32;
+            nacc -= 32;
         }
-        const int total = __shfl_sync(FULL, incl, 31);
-        if (nb) {
-            const uint32_t b = bp + (uint32_t)(incl - nb);
-            const uint32_t q = b >> 5, sh = b & 31;
-            atomicOr(&out[q], v << sh);
-            if (sh + (uint32_t)nb > 32) atomicOr(&out[q + 1], v >> (32 - sh));
-        }
-        bp += (uint32_t)total;
-        pos += t;
-        __syncwarp();
     }
-    return bp;
+    if (nacc > 0) ob[nw] = (uint32_t)acc;
+    return bits;
 }
 
 // Adler sums of n bytes in shared memory (whole CTA).
@@ -253,17 +199,17 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     uint32_t (*ctab)[256] = reinterpret_cast<uint32_t (*)[256]>(sm);
     uint8_t* in = sm + 4096;
     const int in_bytes = lz_in_bytes(max_block);
-    const int ow = lz_out_words(max_block);
+    const int lw = lz_lane_words(max_block);
     uint32_t* outs = reinterpret_cast<uint32_t*>(in + in_bytes);
-    uint32_t* tabs = outs + kLzWarps * ow;
+    uint16_t* tabs = reinterpret_cast<uint16_t*>(outs + kLzThreads * lw);
     __shared__ uint64_t red64[kLzWarps];
     __shared__ uint32_t red32[kLzWarps];
-    __shared__ uint32_t seg_bits[kLzWarps];
+    __shared__ uint32_t wsum[kLzWarps];
     __shared__ uint32_t s_info[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     build_crc_tables(ctab);
-    uint32_t* myout = outs + warp * ow;
-    uint32_t* mytab = tabs + warp * kHashSize;
+    uint16_t* mytab = tabs + warp * kHashSize;
+    uint32_t* myout = outs + tid * lw;
 
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
         BlockOut& bo = blocks[b];
@@ -273,7 +219,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         const uint8_t* src = d.filt + bo.in_off;
         const bool last = ((int)(b - d.blk0) == d.nblocks - 1);
         __syncthreads();
-        // stage the block (+ zero padding) and clear the per-warp state
+        // stage the block (+ zero padding), clear the hash tables
         if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
             for (int i = tid; i < (n >> 4); i += kLzThreads)
                 reinterpret_cast<uint4*>(in)[i] = __ldg(reinterpret_cast<const uint4*>(src) + i);
@@ -282,49 +228,61 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             for (int i = tid; i < n; i += kLzThreads) in[i] = src[i];
         }
         for (int i = n + tid; i < in_bytes; i += kLzThreads) in[i] = 0;
-        for (int i = lane; i < ow; i += 32) myout[i] = 0;
-        for (int i = lane; i < kHashSize; i += 32) mytab[i] = 0;
+        for (int i = tid; i < kLzWarps * kHashSize / 2; i += kLzThreads) reinterpret_cast<uint32_t*>(tabs)[i] = 0u;
         __syncthreads();
         uint32_t s1;
         uint64_t s2;
         cta_adler_sums<kLzThreads>(in, n, s1, s2, red64);
-        // parse
-        const int seg = (n + kLzWarps - 1) / kLzWarps;
-        const int s0 = min(n, warp * seg), se = min(n, s0 + seg);
-        const int rb1 = d.rb + 1;
-        const uint32_t nbits = (s0 < se) ? parse_segment(in, n, s0, se, rb1, mytab, myout, lane) : 0u;
-        if (lane == 0) seg_bits[warp] = nbits;
+        // seed the warp's table from the bytes before its range, oldest first
+        const int sub = lz_sub_bytes(n);
+        const int ws0 = min(n, warp * 32 * sub);
+        for (int q0 = max(0, ws0 - kPrefill); q0 < ws0; q0 += 32) {
+            const int q = q0 + lane;
+            if (q < ws0 && q + 4 <= n) mytab[hash4(ld32u(in, q))] = (uint16_t)(q + 1);
+            __syncwarp();
+        }
+        // parse this thread's sub-range
+        const int s = min(n, tid * sub), e = min(n, s + sub);
+        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, d.rb + 1, mytab, myout) : 0u;
+        // CTA-wide exclusive scan of the bit counts
+        uint32_t incl = nbits;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[warp] = incl;
         __syncthreads();
+        uint32_t wbase = 0, tot = 3;
+        for (int k = 0; k < kLzWarps; k++) {
+            if (k < warp) wbase += wsum[k];
+            tot += wsum[k];
+        }
+        tot += 7;                                                  // end-of-block code
+        const uint32_t off = 3 + wbase + incl - nbits;             // bit offset of this thread's stream
         if (tid == 0) {
-            uint32_t tot = 3;
-            for (int w = 0; w < kLzWarps; w++) tot += seg_bits[w];
-            tot += 7;                                              // end-of-block code
             const uint32_t huff = last ? (tot + 7) / 8 : (tot + 3 + 7) / 8 + 4;
             const uint32_t stored = (uint32_t)n + kStoredHdr;
-            s_info[0] = tot;
             s_info[1] = (huff < stored) ? huff : 0u;               // 0 = stored block
         }
         __syncthreads();
-        const uint32_t tot = s_info[0], huff = s_info[1];
+        const uint32_t huff = s_info[1];
         uint8_t* slot = scratch + (size_t)b * slot_bytes;
         uint32_t crc;
         if (huff) {
-            // stitch the warp bitstreams behind the 3-bit header into `in`
+            // place the 512 bitstreams behind the 3-bit header, into `in`
             uint32_t* region = reinterpret_cast<uint32_t*>(in);
             const int rwords = (int)((huff + 3) / 4) + 2;
             for (int i = tid; i < rwords; i += kLzThreads) region[i] = 0;
             __syncthreads();
-            uint32_t off = 3;
-            for (int w = 0; w < warp; w++) off += seg_bits[w];
             const int nw = (int)((nbits + 31) / 32);
-            for (int j = lane; j < nw; j += 32) {
+            const uint32_t sh = off & 31, q0 = off >> 5;
+            for (int j = 0; j < nw; j++) {
                 const uint32_t v = myout[j];
-                const uint32_t bpos = off + 32u * (uint32_t)j;
-                const uint32_t q = bpos >> 5, sh = bpos & 31;
-                if (v) {
-                    atomicOr(&region[q], v << sh);
-                    if (sh) atomicOr(&region[q + 1], v >> (32 - sh));
-                }
+                if (!v) continue;
+                // first and last words are shared with the neighbouring streams
+                atomicOr(&region[q0 + j], v << sh);
+                if (sh) atomicOr(&region[q0 + j + 1], v >> (32 - sh));
             }
             if (tid == 0) atomicOr(&region[0], last ? 3u : 2u);     // BFINAL, BTYPE = 01
             __syncthreads();

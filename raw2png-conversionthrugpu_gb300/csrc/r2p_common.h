@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #if defined(__CUDACC__)
+#include <cuda_fp16.h>
 #define R2P_HD __host__ __device__ __forceinline__
 #else
 #define R2P_HD static inline
@@ -79,6 +80,36 @@ R2P_HD uint32_t paeth4(uint32_t a, uint32_t b, uint32_t c)
     return (a & sel_a) | (b & sel_b) | (c & sel_c);
 }
 
+#if defined(__CUDA_ARCH__)
+// Device Paeth on packed halves: bytes become fp16 values 1024 + b (a byte
+// permute with 0x64 high bytes), whose differences up to +-510 are exact.
+// pa = |b - c|, pb = |a - c|, pc = |a + b - 2c| and the a, b, c selection
+// order of the PNG definition; the winner's low byte is the predictor.
+// Checked against the scalar definition on all 2^24 (a, b, c).
+__device__ __forceinline__ uint32_t paeth_h2(uint32_t a, uint32_t b, uint32_t c)
+{
+    const __half2 ha = *reinterpret_cast<const __half2*>(&a);
+    const __half2 hb = *reinterpret_cast<const __half2*>(&b);
+    const __half2 hc = *reinterpret_cast<const __half2*>(&c);
+    const __half2 A = __hsub2(ha, hc), B = __hsub2(hb, hc);
+    const __half2 pa = __habs2(B), pb = __habs2(A), pc = __habs2(__hadd2(A, B));
+    const uint32_t ma = __hle2_mask(pa, pb) & __hle2_mask(pa, pc);
+    const uint32_t mb = __hle2_mask(pb, pc);
+    return (a & ma) | (~ma & ((b & mb) | (c & ~mb)));
+}
+
+__device__ __forceinline__ uint32_t paeth4_dev(uint32_t a, uint32_t b, uint32_t c)
+{
+    const uint32_t K = 0x64646464u;
+    const uint32_t lo = paeth_h2(__byte_perm(a, K, 0x4140), __byte_perm(b, K, 0x4140), __byte_perm(c, K, 0x4140));
+    const uint32_t hi = paeth_h2(__byte_perm(a, K, 0x4342), __byte_perm(b, K, 0x4342), __byte_perm(c, K, 0x4342));
+    return __byte_perm(lo, hi, 0x6420);
+}
+#define R2P_PAETH4 paeth4_dev
+#else
+#define R2P_PAETH4 paeth4
+#endif
+
 // Sum over the four bytes of |int8(v)| = min(v, 256 - v), added to acc.
 R2P_HD uint32_t cost4_acc(uint32_t v, uint32_t acc)
 {
@@ -137,7 +168,7 @@ R2P_HD void score_word(Score5& s, uint32_t x, uint32_t a, uint32_t b, uint32_t c
     s.s1 = cost4_acc(sub4(x, a) & mask, s.s1);
     s.s2 = cost4_acc(sub4(x, b) & mask, s.s2);
     s.s3 = cost4_acc(sub4(x, avg4(a, b)) & mask, s.s3);
-    s.s4 = cost4_acc(sub4(x, paeth4(a, b, c)) & mask, s.s4);
+    s.s4 = cost4_acc(sub4(x, R2P_PAETH4(a, b, c)) & mask, s.s4);
 }
 
 // Filtered word for filter type f (0..4).
@@ -148,7 +179,7 @@ R2P_HD uint32_t filter_word(int f, uint32_t x, uint32_t a, uint32_t b, uint32_t 
         case 1: return sub4(x, a);
         case 2: return sub4(x, b);
         case 3: return sub4(x, avg4(a, b));
-        default: return sub4(x, paeth4(a, b, c));
+        default: return sub4(x, R2P_PAETH4(a, b, c));
     }
 }
 

@@ -158,7 +158,7 @@ static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip)
     }
     ip.lut_cap = align_up((uint64_t)entries * esize + 16, 256);
     ip.lreg = filter_lut_region(mode_guess, entries, esize);
-    ip.smem = filter_smem_bytes(d.rb, mode_guess, entries, esize);
+    ip.smem = filter_smem_bytes(d.rb, d.in_pitch, mode_guess, entries, esize);
     if (ip.smem < 0) return set_err(R2P_EINVAL, "row too wide for the filter kernel");
     ip.png_bound = (uint64_t)d.prefix + F + (uint64_t)kStoredHdr * nb + (out_kind == 0 ? kPngSuffix : 4);
     if (F >= (1ull << 32) || ip.png_bound >= (1ull << 31) - 64)
@@ -267,7 +267,7 @@ static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers
     for (int i = 0; i < n; i++) {
         DevImage& d = plans[i].di;
         if (P.smem > 0) {
-            const int T = filter_tile_rows(d.rb, P.smem, plans[i].lreg);
+            const int T = filter_tile_rows(d.rb, d.in_pitch, P.smem, plans[i].lreg);
             const uint64_t ntiles = (d.height + T - 1) / T;
             uint64_t nb = std::min<uint64_t>(ntiles, (uint64_t)P.slots_total);
             if (n > 1) nb = std::min<uint64_t>(ntiles, std::max<uint64_t>(1, (uint64_t)P.slots_total / n + 1));
@@ -573,7 +573,11 @@ int r2p_encode_png(r2p_engine* e, const r2p_image* img, const void* h_pixels, vo
     uint64_t len = 0;
     R2P_CU(cudaMemcpyAsync(&len, d_len, sizeof(len), cudaMemcpyDeviceToHost, s), "length download");
     R2P_CU(cudaStreamSynchronize(s), "sync");
-    if (len == ~0ull) return set_err(R2P_ENOSPC, "png buffer too small");
+    if (len >> 63) {
+        const int st = (int)(len & 0xFF);
+        return set_err(st, st == R2P_ETIMEOUT ? "a bounded device wait gave up (bulk copy did not land)"
+                                              : "png buffer too small");
+    }
     *png_len = (size_t)len;
     if (len > png_cap) return set_err(R2P_ENOSPC, "png_cap too small for the encoded PNG");
     R2P_CU(cudaMemcpyAsync(h_png, d_png, (size_t)len, cudaMemcpyDeviceToHost, s), "png download");

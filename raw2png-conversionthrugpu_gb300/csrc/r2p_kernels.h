@@ -11,10 +11,10 @@ void note_launch();
 
 // k_filter.cu
 cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s);
-cudaError_t launch_window_filter(const DevImage* imgs, const BandItem* items, int nitems, int grid,
+cudaError_t launch_window_filter(DevImage* imgs, const BandItem* items, int nitems, int grid,
                                  int smem, cudaStream_t s);
-int filter_smem_bytes(int rb, int mode, int lut_entries, int lut_esize);
-int filter_tile_rows(int rb, int smem, int lut_region);
+int filter_smem_bytes(int rb, int in_pitch, int mode, int lut_entries, int lut_esize);
+int filter_tile_rows(int rb, int in_pitch, int smem, int lut_region);
 int filter_lut_region(int mode, int lut_entries, int lut_esize);
 int filter_ctas_per_sm(int smem);
 
