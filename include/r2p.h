@@ -91,7 +91,9 @@ typedef struct r2p_engine r2p_engine;
 int  r2p_engine_create(int device, size_t hbm_budget, r2p_engine** out);
 void r2p_engine_destroy(r2p_engine* eng);
 
-/* Upper bound of the PNG size for an image; 0 on invalid geometry. */
+/* Upper bound of the PNG size for an image under any tuning table (it assumes
+ * 1024-byte DEFLATE blocks unless img->block_size is set); 0 on invalid
+ * geometry. */
 size_t r2p_png_bound(const r2p_image* img);
 
 /* Encode one image from host memory to a PNG in host memory (blocking).
@@ -115,6 +117,37 @@ int r2p_encode_png_device(r2p_engine* eng, const r2p_image* img, const void* d_p
 int r2p_encode_batch_device(r2p_engine* eng, int n, const r2p_image* imgs,
                             const void* const* d_pixels, void* const* d_pngs,
                             const size_t* png_caps, uint64_t* d_png_lens, void* stream);
+
+/* Reusable batch: the work list (row bands, DEFLATE blocks) and descriptors of
+ * n images are planned and uploaded once, with the batch's own device
+ * scratch (r2p_batch_device_bytes); r2p_batch_launch then issues only the
+ * stage kernels, and r2p_batch_launch_graph captures that kernel sequence
+ * once as a CUDA graph and replays it.  Pixels and PNG buffers are fixed at
+ * creation.  Replaces the folder batch's per-file encode pool and thread-local
+ * context cache (src/batch_processor.cpp:482-737, src/pipeline.cpp:1527-1561). */
+typedef struct r2p_batch r2p_batch;
+int    r2p_batch_create(r2p_engine* eng, int n, const r2p_image* imgs, const void* const* d_pixels,
+                        void* const* d_pngs, const size_t* png_caps, uint64_t* d_png_lens, r2p_batch** out);
+int    r2p_batch_launch(r2p_batch* b, void* stream);
+int    r2p_batch_launch_graph(r2p_batch* b, void* stream);
+size_t r2p_batch_device_bytes(const r2p_batch* b);
+void   r2p_batch_destroy(r2p_batch* b);
+
+/* Size-class tuning: per class of raw image bytes (sorted, the last class
+ * takes everything larger), the DEFLATE block size used when an image's
+ * block_size is 0, the filter's rows per work item (0 = from occupancy) and
+ * the LZ77 hash-table size (2^10 or 2^11 entries per warp; one per launch,
+ * the value most blocks of the launch were tuned for).  Set from the
+ * autotuner's table; n = 0 restores the built-in one.  Replaces the fixed
+ * strip-height/pool-size defaults (src/main.cpp:165-170, src/pipeline.cpp:1587). */
+typedef struct r2p_tuning {
+    uint64_t max_raw_bytes;
+    int      block_size;
+    int      band_rows;
+    int      hash_bits;
+} r2p_tuning;
+int r2p_engine_set_tuning(r2p_engine* eng, int n, const r2p_tuning* classes);
+int r2p_engine_get_tuning(r2p_engine* eng, int cap, r2p_tuning* out, int* n);
 
 /* Stage entry point: window + adaptive filter of a whole image into
  * height*(row_bytes+1) filtered scanline bytes on the device.  d_prior (may

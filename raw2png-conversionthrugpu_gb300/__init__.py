@@ -68,6 +68,12 @@ class DicomParams(ctypes.Structure):
         return p
 
 
+class Tuning(ctypes.Structure):
+    """r2p_tuning: one image-size class of the autotuned table."""
+    _fields_ = [("max_raw_bytes", ctypes.c_uint64), ("block_size", ctypes.c_int), ("band_rows", ctypes.c_int),
+                ("hash_bits", ctypes.c_int)]
+
+
 class Image(ctypes.Structure):
     """r2p_image."""
     _fields_ = [
@@ -149,6 +155,14 @@ SIGNATURES = {
     "r2p_event_elapsed_ms": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(ctypes.c_float)]),
     "r2p_kernel_launch_count": (ctypes.c_uint64, []),
     "r2p_engine_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "r2p_batch_create": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Image), ctypes.POINTER(_vp),
+                                        ctypes.POINTER(_vp), ctypes.POINTER(_sz), _vp, ctypes.POINTER(_vp)]),
+    "r2p_batch_launch": (ctypes.c_int, [_vp, _vp]),
+    "r2p_batch_launch_graph": (ctypes.c_int, [_vp, _vp]),
+    "r2p_batch_device_bytes": (_sz, [_vp]),
+    "r2p_batch_destroy": (None, [_vp]),
+    "r2p_engine_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Tuning)]),
+    "r2p_engine_get_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_int)]),
     "r2p_engine_stage_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _u64p]),
 }
 
@@ -375,6 +389,20 @@ class Engine:
         check(lib().r2p_engine_stage_times(self.h, ms, n))
         return {STAGES[i]: (ms[i], int(n[i])) for i in range(len(STAGES))}
 
+    def set_tuning(self, classes):
+        """classes: list of (max_raw_bytes, block_size, band_rows, hash_bits)."""
+        arr = (Tuning * len(classes))(*[Tuning(*c) for c in classes]) if classes else None
+        check(lib().r2p_engine_set_tuning(self.h, len(classes), arr))
+
+    def get_tuning(self):
+        arr = (Tuning * 64)()
+        n = ctypes.c_int()
+        check(lib().r2p_engine_get_tuning(self.h, 64, arr, ctypes.byref(n)))
+        return [(t.max_raw_bytes, t.block_size, t.band_rows, t.hash_bits) for t in arr[:n.value]]
+
+    def batch(self, imgs, d_pixels, d_pngs, caps, d_lens):
+        return Batch(self, imgs, d_pixels, d_pngs, caps, d_lens)
+
     # convenience wrappers that move data through host memory (tests)
     def filter_image(self, img, pixels, prior=None):
         px = DeviceBuffer.from_array(np.ascontiguousarray(pixels).view(np.uint8).reshape(-1))
@@ -401,3 +429,39 @@ class Engine:
         res = DeviceBuffer(4)
         (self.adler32_device if kind == "adler32" else self.crc32_device)(src.ptr, data.size, res.ptr)
         return int(res.download(4).view(np.uint32)[0])
+
+
+class Batch:
+    """A planned batch (r2p_batch): launch directly or as a CUDA graph."""
+
+    def __init__(self, engine, imgs, d_pixels, d_pngs, caps, d_lens):
+        n = len(imgs)
+        arr = (Image * n)(*imgs)
+        px = (_vp * n)(*d_pixels)
+        pg = (_vp * n)(*d_pngs)
+        cp = (_sz * n)(*caps)
+        p = _vp()
+        check(lib().r2p_batch_create(engine.h, n, arr, px, pg, cp, d_lens, ctypes.byref(p)))
+        self.h = p.value
+        self.engine = engine
+
+    @property
+    def device_bytes(self):
+        return lib().r2p_batch_device_bytes(self.h)
+
+    def launch(self, stream=None):
+        check(lib().r2p_batch_launch(self.h, _sp(stream)))
+
+    def launch_graph(self, stream=None):
+        check(lib().r2p_batch_launch_graph(self.h, _sp(stream)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().r2p_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,81 @@
+"""Autotuner for the size-class table (r2p_tuning).
+
+For each image-size class of the batched CT workload it times candidate
+(DEFLATE block size, filter rows per work item, LZ77 hash-table bits) on a
+planned batch of that class, replayed as a CUDA graph, keeps the fastest
+candidate, and writes the table that Engine.set_tuning() takes.  Runs on the
+GPU; `python -m`-style entry: python raw2png-conversionthrugpu_gb300/autotune.py
+[--out path.json].
+"""
+import json
+import os
+import sys
+
+CLASSES = [(256, 256), (512, 512), (1024, 1024), (2048, 2500), (3072, 3072)]
+CANDIDATES = [(65520, 0, 11), (65520, 0, 10), (32752, 0, 11), (32752, 0, 10), (16368, 0, 10),
+              (65520, 64, 11), (32752, 32, 10)]
+DEFAULT_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_gb300.json")
+
+
+def class_bounds():
+    """Upper raw-byte bound of each class: halfway to the next class."""
+    sizes = [w * h * 2 for w, h in CLASSES]
+    return [(sizes[i] + sizes[i + 1]) // 2 for i in range(len(sizes) - 1)] + [2 ** 62]
+
+
+def tune(r2p, W, reps=5, target_bytes=160 << 20, log=print):
+    import torch
+    eng = r2p.Engine(0)
+    stream = r2p.Stream()
+    table = []
+    for (w, h), bound in zip(CLASSES, class_bounds()):
+        k = max(4, min(256, target_bytes // (w * h * 2)))
+        raws = [W.ct_phantom_torch(7000 + i, w, h) for i in range(k)]
+        imgs = [W.image_ct8(w, h, 40.0 + 10 * i, 400.0 + 5 * i, level=1) for i in range(k)]
+        caps = [r2p.png_bound(im) for im in imgs]
+        outs = [torch.empty(c, dtype=torch.uint8, device="cuda") for c in caps]
+        lens = torch.zeros(k, dtype=torch.int64, device="cuda")
+        torch.cuda.synchronize()
+        best = None
+        for cand in CANDIDATES:
+            eng.set_tuning([(2 ** 62, cand[0], cand[1], cand[2])])
+            b = eng.batch(imgs, [t.data_ptr() for t in raws], [t.data_ptr() for t in outs], caps, lens.data_ptr())
+            b.launch_graph(stream)
+            b.launch_graph(stream)
+            e0, e1 = r2p.Event(), r2p.Event()
+            times = []
+            for _ in range(reps):
+                e0.record(stream)
+                b.launch_graph(stream)
+                e1.record(stream)
+                times.append(e0.elapsed_ms(e1))
+            stream.sync()
+            b.close()
+            ms = sorted(times)[len(times) // 2]
+            log("class %dx%d x%d  block %d band_rows %d hash_bits %d: %.3f ms (%.1f images/s)"
+                % (w, h, k, cand[0], cand[1], cand[2], ms, k / ms * 1e3))
+            if best is None or ms < best[0]:
+                best = (ms, cand)
+        table.append((bound, best[1][0], best[1][1], best[1][2]))
+        del raws, outs
+    eng.close()
+    return table
+
+
+def main():
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import __graft_entry__ as g
+    r2p = g.load_package()
+    from raw2png_gb300 import workloads as W
+    out = sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else DEFAULT_OUT
+    table = tune(r2p, W)
+    with open(out, "w") as f:
+        json.dump({"device": "GB300", "workload": "CT phantom slices, 8-bit window, LZ77 level 1",
+                   "fields": ["max_raw_bytes", "block_size", "band_rows", "hash_bits"], "classes": table}, f,
+                  indent=1)
+    print("wrote", out, table)
+
+
+if __name__ == "__main__":
+    main()

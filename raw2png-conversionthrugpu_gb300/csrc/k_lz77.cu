@@ -32,8 +32,6 @@ namespace r2p {
 
 constexpr int kLzWarps = 16;
 constexpr int kLzThreads = kLzWarps * 32;
-constexpr int kHashBits = 11;
-constexpr int kHashSize = 1 << kHashBits;
 constexpr int kPrefill = 4096;        // history bytes hashed before a warp's range
 constexpr int kMaxDist = 32768;
 constexpr int kMaxMatch = 258;
@@ -50,9 +48,10 @@ __host__ __device__ inline int lz_sub_bytes(int block_size)
 __host__ __device__ inline int lz_lane_words(int block_size) { return ((lz_sub_bytes(block_size) * 9 + 31) / 32 + 2) | 1; }
 __host__ __device__ inline int lz_in_bytes(int block_size) { return ((block_size + 15) & ~15) + 64; }
 
-static int lz_smem_bytes(int block_size)
+static int lz_smem_bytes(int block_size, int hash_bits)
 {
-    return 4096 + lz_in_bytes(block_size) + kLzThreads * lz_lane_words(block_size) * 4 + kLzWarps * kHashSize * 2 + 256;
+    return 4096 + lz_in_bytes(block_size) + kLzThreads * lz_lane_words(block_size) * 4 +
+           kLzWarps * (1 << hash_bits) * 2 + 256;
 }
 
 uint64_t lz77_slot_bytes(int block_size) { return (uint64_t)((block_size + kStoredHdr + 64 + 255) & ~255); }
@@ -65,7 +64,8 @@ __device__ __forceinline__ uint32_t ld32u(const uint8_t* base, int p)
     return fshr(w[q], w[q + 1], (uint32_t)(p & 3) << 3);
 }
 
-__device__ __forceinline__ uint32_t hash4(uint32_t v) { return (v * 2654435761u) >> (32 - kHashBits); }
+template <int HB>
+__device__ __forceinline__ uint32_t hash4(uint32_t v) { return (v * 2654435761u) >> (32 - HB); }
 
 // Fixed-Huffman code of a literal byte: reversed code and its length.
 __device__ __forceinline__ void lit_code(uint32_t b, uint32_t& v, int& n)
@@ -111,6 +111,7 @@ __device__ __forceinline__ void match_code(int len, int dist, uint32_t& v, int& 
 // Greedy parse of in[s, e) by one thread into the word buffer `ob`.
 // `tab` is the warp's shared hash table (latest position + 1 per hash).
 // Returns the number of bits written; the last partial word is stored too.
+template <int HB>
 __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, uint16_t* tab, uint32_t* ob)
 {
     const bool vert = rb1 > 1 && rb1 <= kMaxDist;
@@ -122,7 +123,7 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, uint16_
         int L = 0, D = 0;
         if (p + 4 <= e) {
             const uint32_t w = ld32u(in, p);
-            const uint32_t h = hash4(w);
+            const uint32_t h = hash4<HB>(w);
             const int t = tab[h];
             tab[h] = (uint16_t)(p + 1);
             if (p > 0 && w == (uint32_t)in[p - 1] * 0x01010101u) {
@@ -191,6 +192,7 @@ __device__ void cta_adler_sums(const uint8_t* buf, int n, uint32_t& s1_out, uint
     s2_out = cta_sum64<NT>(s2, red64);
 }
 
+template <int HB>
 __global__ void __launch_bounds__(kLzThreads, 1)
 k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int max_block,
               uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
@@ -207,6 +209,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     __shared__ uint32_t wsum[kLzWarps];
     __shared__ uint32_t s_info[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kHashSize = 1 << HB;
     build_crc_tables(ctab);
     uint16_t* mytab = tabs + warp * kHashSize;
     uint32_t* myout = outs + tid * lw;
@@ -238,12 +241,12 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         const int ws0 = min(n, warp * 32 * sub);
         for (int q0 = max(0, ws0 - kPrefill); q0 < ws0; q0 += 32) {
             const int q = q0 + lane;
-            if (q < ws0 && q + 4 <= n) mytab[hash4(ld32u(in, q))] = (uint16_t)(q + 1);
+            if (q < ws0 && q + 4 <= n) mytab[hash4<HB>(ld32u(in, q))] = (uint16_t)(q + 1);
             __syncwarp();
         }
         // parse this thread's sub-range
         const int s = min(n, tid * sub), e = min(n, s + sub);
-        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, d.rb + 1, mytab, myout) : 0u;
+        const uint32_t nbits = (s < e) ? parse_lane<HB>(in, s, e, d.rb + 1, mytab, myout) : 0u;
         // CTA-wide exclusive scan of the bit counts
         uint32_t incl = nbits;
 #pragma unroll
@@ -317,15 +320,24 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     }
 }
 
-cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
-                        uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s)
+template <int HB>
+static cudaError_t launch_lz77_hb(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
+                                  uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s)
 {
-    const int smem = lz_smem_bytes(max_block);
-    cudaError_t e = cudaFuncSetAttribute(k_lz77_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int smem = lz_smem_bytes(max_block, HB);
+    cudaError_t e = cudaFuncSetAttribute(k_lz77_blocks<HB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    k_lz77_blocks<<<grid, kLzThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    k_lz77_blocks<HB><<<grid, kLzThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
     note_launch();
     return cudaGetLastError();
+}
+
+cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
+                        uint64_t slot_bytes, const uint32_t* xpow, int grid, int hash_bits, cudaStream_t s)
+{
+    if (hash_bits == 10)
+        return launch_lz77_hb<10>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow, grid, s);
+    return launch_lz77_hb<11>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow, grid, s);
 }
 
 }  // namespace r2p

@@ -27,6 +27,11 @@ namespace r2p {
 
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// a graph replay launches the captured kernels again
+static void note_launch_graph(bool stored, bool lz)
+{
+    g_launches.fetch_add(3u + (stored ? 1u : 0u) + (lz ? 2u : 0u), std::memory_order_relaxed);
+}
 
 static thread_local std::string t_last_error;
 
@@ -77,16 +82,23 @@ struct ImgPlan {
     uint64_t png_bound = 0;
     int smem = 0;      // filter smem wanted
     int lreg = 0;      // worst-case LUT region
+    int band_rows = 0; // rows per filter work item (0 = from occupancy)
+    int hash_bits = 11;
 };
 
-static int auto_block_size(const r2p_image& im, uint64_t F)
+// Built-in size-class table (every class: 64 KiB blocks, bands from
+// occupancy, 2^11-entry LZ77 hash tables); engines may load an autotuned one.
+static const std::vector<r2p_tuning> kDefaultTuning = {{~0ull, kBlock64, 0, 11}};
+
+static const r2p_tuning& tune_for(const std::vector<r2p_tuning>& t, uint64_t raw_bytes)
 {
-    (void)im;
-    (void)F;
-    return kBlock64;
+    for (const auto& c : t)
+        if (raw_bytes <= c.max_raw_bytes) return c;
+    return t.back();
 }
 
-static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip)
+static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip,
+                      const std::vector<r2p_tuning>& tune = kDefaultTuning)
 {
     if (im.width < 1 || im.height < 1) return set_err(R2P_EINVAL, "width and height must be >= 1");
     if (im.channels != 1 && im.channels != 3 && im.channels != 4)
@@ -137,7 +149,11 @@ static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip)
     d.req_mode = im.window_mode;
     d.dp = im.dicom;
     d.level = im.level;
-    int bs = im.block_size ? im.block_size : auto_block_size(im, F);
+    const uint64_t raw_total = pitch * im.height;
+    const r2p_tuning& tc = tune_for(tune, raw_total);
+    int bs = im.block_size ? im.block_size : tc.block_size;
+    ip.band_rows = tc.band_rows;
+    ip.hash_bits = tc.hash_bits;
     if (bs < 1024 || bs > kBlock64 || (bs & 15)) return set_err(R2P_EINVAL, "block_size must be a multiple of 16 in [1024, 65520]");
     d.block_size = bs;
     const uint64_t nb = (F + bs - 1) / bs;
@@ -177,10 +193,15 @@ struct r2p_engine {
     uint32_t* d_xpow = nullptr;
     uint8_t* arena = nullptr;
     size_t arena_cap = 0;
-    uint8_t* h_stage = nullptr;
-    size_t stage_cap = 0;
+    // pinned staging ring for descriptor uploads: the host may run up to
+    // kStageRing calls ahead of the device before reusing a slot
+    static constexpr int kStageRing = 8;
+    uint8_t* h_stage[kStageRing] = {};
+    size_t stage_cap[kStageRing] = {};
+    cudaEvent_t staged[kStageRing] = {};   // upload of the call that last used the slot
+    bool stage_used[kStageRing] = {};
+    int stage_idx = 0;
     cudaEvent_t done = nullptr;     // last kernel of the previous call
-    cudaEvent_t staged = nullptr;   // descriptor upload of the previous call
     bool have_done = false;
     std::mutex mu;
     // stage timing (events between stage launches on the call's stream)
@@ -188,7 +209,9 @@ struct r2p_engine {
     std::vector<std::vector<cudaEvent_t>> trec;   // per timed call: R2P_STAGE_COUNT + 1 events
     std::vector<uint32_t> tmask;                  // stages each timed call launched
     size_t tused = 0;
+    std::vector<r2p_tuning> tuning = kDefaultTuning;
 };
+
 
 namespace r2p {
 
@@ -230,19 +253,25 @@ static int ensure_arena(r2p_engine* e, size_t need)
     return R2P_OK;
 }
 
-static int ensure_stage(r2p_engine* e, size_t need)
+// Take the next staging slot, waiting for the upload that last used it and
+// growing it to `need` bytes.
+static int ensure_stage(r2p_engine* e, size_t need, int* slot)
 {
-    if (e->have_done) R2P_CU(cudaEventSynchronize(e->staged), "staging wait");
-    if (need <= e->stage_cap) return R2P_OK;
-    if (e->h_stage) cudaFreeHost(e->h_stage);
-    e->h_stage = nullptr;
-    size_t cap = align_up(need * 2, 1 << 16);
-    R2P_CU(cudaMallocHost(&e->h_stage, cap), "staging cudaMallocHost");
-    e->stage_cap = cap;
+    const int k = e->stage_idx;
+    if (e->stage_used[k]) R2P_CU(cudaEventSynchronize(e->staged[k]), "staging wait");
+    if (need > e->stage_cap[k]) {
+        if (e->h_stage[k]) cudaFreeHost(e->h_stage[k]);
+        e->h_stage[k] = nullptr;
+        e->stage_cap[k] = 0;
+        const size_t cap = align_up(need * 2, 1 << 16);
+        R2P_CU(cudaMallocHost(&e->h_stage[k], cap), "staging cudaMallocHost");
+        e->stage_cap[k] = cap;
+    }
+    *slot = k;
     return R2P_OK;
 }
 
-// One call's work list and arena layout.
+// One call's work list and memory layout.
 struct Prepared {
     std::vector<BandItem> items;
     std::vector<BlockOut> blocks;
@@ -251,27 +280,34 @@ struct Prepared {
     bool any_lz = false, any_stored = false;
     uint64_t slot = 0;
     size_t o_img = 0, o_items = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0, o_extra = 0;
+    size_t total = 0;
+    int hash_bits = 11;
+    int stage_slot = 0;
 };
 
-// Plan the work list and arena layout for n images, make sure the arena and
-// staging area are large enough, and order this call after the previous one
-// on `s`.  *extra receives extra_bytes of arena space for the caller.
-static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
-                   cudaStream_t s, Prepared& P, uint8_t** extra)
+// Work list and memory layout of one call (or one batch) over n images.
+static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
+                      Prepared& P)
 {
     const int n = (int)plans.size();
     for (auto& p : plans) P.smem = std::max(P.smem, p.smem);
     const int cps = P.smem > 0 ? filter_ctas_per_sm(P.smem) : 1;
     P.slots_total = e->nsm * cps;
     uint64_t lut_total = 0, filt_total = 0;
+    int hb_votes[2] = {0, 0};
     for (int i = 0; i < n; i++) {
         DevImage& d = plans[i].di;
         if (P.smem > 0) {
             const int T = filter_tile_rows(d.rb, d.in_pitch, P.smem, plans[i].lreg);
             const uint64_t ntiles = (d.height + T - 1) / T;
-            uint64_t nb = std::min<uint64_t>(ntiles, (uint64_t)P.slots_total);
-            if (n > 1) nb = std::min<uint64_t>(ntiles, std::max<uint64_t>(1, (uint64_t)P.slots_total / n + 1));
-            const uint64_t band_rows = ((ntiles + nb - 1) / nb) * T;
+            uint64_t band_rows;
+            if (plans[i].band_rows > 0) {
+                band_rows = ((uint64_t)plans[i].band_rows + T - 1) / T * T;    // tuned, whole tiles
+            } else {
+                uint64_t nb = std::min<uint64_t>(ntiles, (uint64_t)P.slots_total);
+                if (n > 1) nb = std::min<uint64_t>(ntiles, std::max<uint64_t>(1, (uint64_t)P.slots_total / n + 1));
+                band_rows = ((ntiles + nb - 1) / nb) * T;
+            }
             for (uint64_t r = 0; r < d.height; r += band_rows)
                 P.items.push_back(BandItem{(uint32_t)i, (uint32_t)r,
                                            (uint32_t)std::min<uint64_t>(d.height, r + band_rows)});
@@ -288,9 +324,12 @@ static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers
         P.nblk += (uint32_t)d.nblocks;
         P.max_block = std::max(P.max_block, d.block_size);
         if (d.level == 0) P.any_stored = true; else P.any_lz = true;
+        if (d.level > 0) hb_votes[plans[i].hash_bits == 10 ? 0 : 1] += d.nblocks;
         lut_total += plans[i].lut_cap;
         if (!cb.filt[i]) filt_total += align_up(d.filt_bytes + 64, 256);
     }
+    // one hash-table size per launch: the one most blocks were tuned for
+    P.hash_bits = hb_votes[0] > hb_votes[1] ? 10 : 11;
     P.slot = P.any_lz ? lz77_slot_bytes(P.max_block) : 0;
     Layout L;
     P.o_img = L.take(sizeof(DevImage) * n);
@@ -301,23 +340,14 @@ static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers
     P.o_filt = L.take(filt_total);
     P.o_scratch = L.take(P.slot * P.nblk);
     P.o_extra = L.take(extra_bytes);
-    int rc = ensure_arena(e, L.off);
-    if (rc) return rc;
-    rc = ensure_stage(e, P.desc_bytes);
-    if (rc) return rc;
-    if (e->have_done) R2P_CU(cudaStreamWaitEvent(s, e->done, 0), "order calls");
-    if (extra) *extra = e->arena + P.o_extra;
-    return R2P_OK;
+    P.total = L.off;
 }
 
-// Fill the device pointers, upload the descriptors and launch the stages.
-static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, Prepared& P, int stages,
-                  cudaStream_t s)
+// Point the image descriptors at their buffers inside memory base A.
+static void fill_pointers(std::vector<ImgPlan>& plans, const CallBuffers& cb, const Prepared& P, uint8_t* A)
 {
-    const int n = (int)plans.size();
-    uint8_t* A = e->arena;
     uint64_t lut_off = P.o_lut, filt_off = P.o_filt;
-    for (int i = 0; i < n; i++) {
+    for (size_t i = 0; i < plans.size(); i++) {
         DevImage& d = plans[i].di;
         d.lut = A + lut_off;
         lut_off += plans[i].lut_cap;
@@ -333,48 +363,45 @@ static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers&
         d.png_cap = cb.out_cap[i];
         d.png_len = cb.out_len[i];
     }
-    uint8_t* H = e->h_stage;
-    for (int i = 0; i < n; i++) memcpy(H + P.o_img + i * sizeof(DevImage), &plans[i].di, sizeof(DevImage));
+}
+
+static void write_descriptors(uint8_t* H, const std::vector<ImgPlan>& plans, const Prepared& P)
+{
+    for (size_t i = 0; i < plans.size(); i++) memcpy(H + P.o_img + i * sizeof(DevImage), &plans[i].di, sizeof(DevImage));
     if (!P.items.empty()) memcpy(H + P.o_items, P.items.data(), P.items.size() * sizeof(BandItem));
     if (!P.blocks.empty()) memcpy(H + P.o_blocks, P.blocks.data(), P.blocks.size() * sizeof(BlockOut));
-    R2P_CU(cudaMemcpyAsync(A, H, P.desc_bytes, cudaMemcpyHostToDevice, s), "descriptor upload");
-    R2P_CU(cudaEventRecord(e->staged, s), "event");
+}
+
+// Launch the stage kernels over a planned, uploaded work list at base A.
+// With tmask != null, tev[k] is recorded before stage k (and tev[6] after
+// the last) and *tmask gets the stages that ran.
+static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stages, cudaStream_t s,
+                         cudaEvent_t* tev, uint32_t* tmask)
+{
     DevImage* dimg = reinterpret_cast<DevImage*>(A + P.o_img);
     BandItem* ditems = reinterpret_cast<BandItem*>(A + P.o_items);
     BlockOut* dblocks = reinterpret_cast<BlockOut*>(A + P.o_blocks);
-    std::vector<cudaEvent_t>* tev = nullptr;
-    if (e->timing) {
-        if (e->tused == e->trec.size()) {
-            std::vector<cudaEvent_t> v(R2P_STAGE_COUNT + 1);
-            for (auto& ev : v) R2P_CU(cudaEventCreate(&ev), "cudaEventCreate");
-            e->trec.push_back(v);
-            e->tmask.push_back(0);
-        }
-        tev = &e->trec[e->tused];
-        e->tmask[e->tused] = 0;
-        e->tused++;
-    }
-    // event k marks the start of stage k; a skipped stage records an empty interval
     auto mark = [&](int k, bool ran) -> cudaError_t {
         if (!tev) return cudaSuccess;
-        if (ran) e->tmask[e->tused - 1] |= 1u << (k - 1);
-        return cudaEventRecord((*tev)[k], s);
+        if (ran) *tmask |= 1u << (k - 1);
+        return cudaEventRecord(tev[k], s);
     };
+    const bool filt = (stages & ST_FILTER) != 0, defl = (stages & ST_DEFLATE) != 0;
     R2P_CU(mark(0, false), "event");
-    if (stages & ST_FILTER) R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
-    R2P_CU(mark(1, (stages & ST_FILTER) != 0), "event");
-    if (stages & ST_FILTER) {
+    if (filt) R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
+    R2P_CU(mark(1, filt), "event");
+    if (filt) {
         const int grid = (int)std::min<size_t>(P.items.size(), (size_t)P.slots_total);
         R2P_CU(launch_window_filter(dimg, ditems, (int)P.items.size(), grid, P.smem, s), "k_window_filter");
     }
-    R2P_CU(mark(2, (stages & ST_FILTER) != 0), "event");
-    const bool defl = (stages & ST_DEFLATE) != 0;
+    R2P_CU(mark(2, filt), "event");
     const int bgrid = (int)std::min<uint64_t>(P.nblk, (uint64_t)e->nsm * 8);
     if (defl && P.any_stored)
         R2P_CU(launch_stored(dimg, dblocks, (int)P.nblk, P.max_block, e->d_xpow, bgrid, s), "k_stored_blocks");
     R2P_CU(mark(3, defl && P.any_stored), "event");
     if (defl && P.any_lz)
-        R2P_CU(launch_lz77(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, bgrid, s),
+        R2P_CU(launch_lz77(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, bgrid,
+                           P.hash_bits, s),
                "k_lz77_blocks");
     R2P_CU(mark(4, defl && P.any_lz), "event");
     if (defl) R2P_CU(launch_finalize(dimg, n, dblocks, e->d_xpow, s), "k_finalize");
@@ -382,6 +409,54 @@ static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers&
     if (defl && P.any_lz)
         R2P_CU(launch_copy_blocks(dimg, dblocks, (int)P.nblk, A + P.o_scratch, P.slot, bgrid, s), "k_copy_blocks");
     R2P_CU(mark(6, defl && P.any_lz), "event");
+    return R2P_OK;
+}
+
+// Plan into the engine arena, make sure it and the staging area are large
+// enough, and order this call after the previous one on `s`.  *extra
+// receives extra_bytes of arena space for the caller.
+static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
+                   cudaStream_t s, Prepared& P, uint8_t** extra)
+{
+    plan_work(e, plans, cb, extra_bytes, P);
+    int rc = ensure_arena(e, P.total);
+    if (rc) return rc;
+    rc = ensure_stage(e, P.desc_bytes, &P.stage_slot);
+    if (rc) return rc;
+    if (e->have_done) R2P_CU(cudaStreamWaitEvent(s, e->done, 0), "order calls");
+    if (extra) *extra = e->arena + P.o_extra;
+    return R2P_OK;
+}
+
+// Fill the device pointers, upload the descriptors and launch the stages.
+static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, Prepared& P, int stages,
+                  cudaStream_t s)
+{
+    const int n = (int)plans.size();
+    uint8_t* A = e->arena;
+    fill_pointers(plans, cb, P, A);
+    const int k = P.stage_slot;
+    write_descriptors(e->h_stage[k], plans, P);
+    R2P_CU(cudaMemcpyAsync(A, e->h_stage[k], P.desc_bytes, cudaMemcpyHostToDevice, s), "descriptor upload");
+    R2P_CU(cudaEventRecord(e->staged[k], s), "event");
+    e->stage_used[k] = true;
+    e->stage_idx = (k + 1) % r2p_engine::kStageRing;
+    cudaEvent_t* tev = nullptr;
+    uint32_t* tmask = nullptr;
+    if (e->timing) {
+        if (e->tused == e->trec.size()) {
+            std::vector<cudaEvent_t> v(R2P_STAGE_COUNT + 1);
+            for (auto& ev : v) R2P_CU(cudaEventCreate(&ev), "cudaEventCreate");
+            e->trec.push_back(v);
+            e->tmask.push_back(0);
+        }
+        tev = e->trec[e->tused].data();
+        e->tmask[e->tused] = 0;
+        tmask = &e->tmask[e->tused];
+        e->tused++;
+    }
+    int rc = launch_stages(e, n, P, A, stages, s, tev, tmask);
+    if (rc) return rc;
     R2P_CU(cudaEventRecord(e->done, s), "event");
     e->have_done = true;
     return R2P_OK;
@@ -402,6 +477,17 @@ static int bind(r2p_engine* e)
 }
 
 }  // namespace r2p
+
+struct r2p_batch {
+    r2p_engine* eng = nullptr;
+    int n = 0;
+    std::vector<ImgPlan> plans;
+    CallBuffers cb;
+    Prepared P;
+    uint8_t* mem = nullptr;           // descriptors + tables + scratch, owned
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
 
 // status message hook for the other translation units of the library
 int r2p_internal_set_error(int code, const char* msg) { return r2p::set_err(code, msg); }
@@ -450,7 +536,8 @@ int r2p_engine_create(int device, size_t hbm_budget, r2p_engine** out)
     if (ce == cudaSuccess) ce = cudaMalloc(&e->d_xpow, tab.size() * 4);
     if (ce == cudaSuccess) ce = cudaMemcpy(e->d_xpow, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming);
-    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->staged, cudaEventDisableTiming);
+    for (int k = 0; k < r2p_engine::kStageRing && ce == cudaSuccess; k++)
+        ce = cudaEventCreateWithFlags(&e->staged[k], cudaEventDisableTiming);
     if (ce != cudaSuccess) {
         r2p_engine_destroy(e);
         return cuda_err(ce, "r2p_engine_create");
@@ -466,9 +553,11 @@ void r2p_engine_destroy(r2p_engine* e)
     if (e->have_done) cudaEventSynchronize(e->done);
     if (e->arena) cudaFree(e->arena);
     if (e->d_xpow) cudaFree(e->d_xpow);
-    if (e->h_stage) cudaFreeHost(e->h_stage);
+    for (int k = 0; k < r2p_engine::kStageRing; k++) {
+        if (e->h_stage[k]) cudaFreeHost(e->h_stage[k]);
+        if (e->staged[k]) cudaEventDestroy(e->staged[k]);
+    }
     if (e->done) cudaEventDestroy(e->done);
-    if (e->staged) cudaEventDestroy(e->staged);
     for (auto& v : e->trec)
         for (auto ev : v) cudaEventDestroy(ev);
     delete e;
@@ -477,8 +566,13 @@ void r2p_engine_destroy(r2p_engine* e)
 size_t r2p_png_bound(const r2p_image* img)
 {
     if (!img) return 0;
+    // Any engine's tuning table may pick blocks down to 1024 bytes, each with
+    // its 5-byte stored-block header, so bound with the smallest block unless
+    // the image fixes its block size.
+    r2p_image im = *img;
+    if (im.block_size == 0) im.block_size = 1024;
     ImgPlan ip;
-    if (plan_image(*img, 0, ip)) return 0;
+    if (plan_image(im, 0, ip)) return 0;
     return (size_t)ip.png_bound;
 }
 
@@ -498,7 +592,7 @@ int r2p_encode_png_device(r2p_engine* e, const r2p_image* img, const void* d_pix
     int rc = bind(e);
     if (rc) return rc;
     std::vector<ImgPlan> plans(1);
-    rc = plan_image(*img, 0, plans[0]);
+    rc = plan_image(*img, 0, plans[0], e->tuning);
     if (rc) return rc;
     if (png_cap < plans[0].png_bound) return set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
     CallBuffers cb;
@@ -522,7 +616,7 @@ int r2p_encode_batch_device(r2p_engine* e, int n, const r2p_image* imgs, const v
     std::vector<ImgPlan> plans((size_t)n);
     CallBuffers cb;
     for (int i = 0; i < n; i++) {
-        rc = plan_image(imgs[i], 0, plans[i]);
+        rc = plan_image(imgs[i], 0, plans[i], e->tuning);
         if (rc) return rc;
         if (png_caps[i] < plans[i].png_bound) return set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
         if (!d_pixels[i] || !d_pngs[i]) return set_err(R2P_EINVAL, "NULL buffer");
@@ -544,7 +638,7 @@ int r2p_encode_png(r2p_engine* e, const r2p_image* img, const void* h_pixels, vo
     int rc = bind(e);
     if (rc) return rc;
     std::vector<ImgPlan> plans(1);
-    rc = plan_image(*img, 0, plans[0]);
+    rc = plan_image(*img, 0, plans[0], e->tuning);
     if (rc) return rc;
     const size_t raw_bytes = (size_t)plans[0].raw_bytes;
     const size_t bound = (size_t)plans[0].png_bound;
@@ -593,7 +687,7 @@ int r2p_window_filter_device(r2p_engine* e, const r2p_image* img, const void* d_
     int rc = bind(e);
     if (rc) return rc;
     std::vector<ImgPlan> plans(1);
-    rc = plan_image(*img, 0, plans[0]);
+    rc = plan_image(*img, 0, plans[0], e->tuning);
     if (rc) return rc;
     CallBuffers cb;
     cb.raw = {static_cast<const uint8_t*>(d_pixels)};
@@ -709,6 +803,134 @@ int r2p_engine_stage_times(r2p_engine* e, double* ms, uint64_t* launches)
     }
     e->tused = 0;
     return R2P_OK;
+}
+
+
+int r2p_engine_set_tuning(r2p_engine* e, int n, const r2p_tuning* classes)
+{
+    if (!e || n < 0 || (n > 0 && !classes)) return set_err(R2P_EINVAL, "bad tuning table");
+    std::vector<r2p_tuning> t;
+    for (int i = 0; i < n; i++) {
+        const r2p_tuning& c = classes[i];
+        if (c.block_size < 1024 || c.block_size > kBlock64 || (c.block_size & 15) || c.band_rows < 0 ||
+            (c.hash_bits != 10 && c.hash_bits != 11) || (i > 0 && c.max_raw_bytes <= classes[i - 1].max_raw_bytes))
+            return set_err(R2P_EINVAL, "tuning class out of range or not sorted by max_raw_bytes");
+        t.push_back(c);
+    }
+    if (t.empty()) t = kDefaultTuning;
+    t.back().max_raw_bytes = ~0ull;   // the last class takes everything larger
+    std::lock_guard<std::mutex> lk(e->mu);
+    e->tuning = t;
+    return R2P_OK;
+}
+
+int r2p_engine_get_tuning(r2p_engine* e, int cap, r2p_tuning* out, int* n)
+{
+    if (!e || !n || (cap > 0 && !out)) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    *n = (int)e->tuning.size();
+    for (int i = 0; i < cap && i < *n; i++) out[i] = e->tuning[i];
+    return R2P_OK;
+}
+
+int r2p_batch_create(r2p_engine* e, int n, const r2p_image* imgs, const void* const* d_pixels, void* const* d_pngs,
+                     const size_t* png_caps, uint64_t* d_png_lens, r2p_batch** out)
+{
+    if (!e || n < 1 || !imgs || !d_pixels || !d_pngs || !png_caps || !d_png_lens || !out)
+        return set_err(R2P_EINVAL, "NULL argument");
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    r2p_batch* b = new r2p_batch();
+    b->eng = e;
+    b->n = n;
+    b->plans.resize((size_t)n);
+    for (int i = 0; i < n; i++) {
+        rc = plan_image(imgs[i], 0, b->plans[i], e->tuning);
+        if (!rc && png_caps[i] < b->plans[i].png_bound) rc = set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
+        if (!rc && (!d_pixels[i] || !d_pngs[i])) rc = set_err(R2P_EINVAL, "NULL buffer");
+        if (rc) { delete b; return rc; }
+        b->cb.raw.push_back(static_cast<const uint8_t*>(d_pixels[i]));
+        b->cb.filt.push_back(nullptr);
+        b->cb.prior.push_back(nullptr);
+        b->cb.out.push_back(static_cast<uint8_t*>(d_pngs[i]));
+        b->cb.out_cap.push_back(png_caps[i]);
+        b->cb.out_len.push_back(d_png_lens + i);
+    }
+    plan_work(e, b->plans, b->cb, 0, b->P);
+    if (e->budget && b->P.total > e->budget) {
+        delete b;
+        return set_err(R2P_EBUDGET, "batch exceeds the engine's HBM budget");
+    }
+    cudaError_t ce = cudaMalloc(&b->mem, b->P.total);
+    if (ce != cudaSuccess) {
+        delete b;
+        return cuda_err(ce, "batch cudaMalloc");
+    }
+    fill_pointers(b->plans, b->cb, b->P, b->mem);
+    std::vector<uint8_t> host(b->P.desc_bytes);
+    write_descriptors(host.data(), b->plans, b->P);
+    ce = cudaMemcpy(b->mem, host.data(), b->P.desc_bytes, cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        cudaFree(b->mem);
+        delete b;
+        return cuda_err(ce, "batch descriptor upload");
+    }
+    *out = b;
+    return R2P_OK;
+}
+
+int r2p_batch_launch(r2p_batch* b, void* stream)
+{
+    if (!b) return set_err(R2P_EINVAL, "NULL batch");
+    int rc = bind(b->eng);
+    if (rc) return rc;
+    return launch_stages(b->eng, b->n, b->P, b->mem, ST_ALL, static_cast<cudaStream_t>(stream), nullptr, nullptr);
+}
+
+int r2p_batch_launch_graph(r2p_batch* b, void* stream)
+{
+    if (!b) return set_err(R2P_EINVAL, "NULL batch");
+    int rc = bind(b->eng);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!b->exec) {
+        // capture on a private stream so the caller's stream state is untouched
+        cudaStream_t cs;
+        R2P_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
+        cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+            rc = launch_stages(b->eng, b->n, b->P, b->mem, ST_ALL, cs, nullptr, nullptr);
+            cudaGraph_t g = nullptr;
+            ce = cudaStreamEndCapture(cs, &g);
+            if (!rc && ce == cudaSuccess) {
+                b->graph = g;
+                ce = cudaGraphInstantiate(&b->exec, g, 0);
+            } else if (g) {
+                cudaGraphDestroy(g);
+            }
+        }
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (ce != cudaSuccess) return cuda_err(ce, "graph capture");
+    }
+    R2P_CU(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
+    note_launch_graph(b->P.any_stored, b->P.any_lz);
+    return R2P_OK;
+}
+
+size_t r2p_batch_device_bytes(const r2p_batch* b) { return b ? b->P.total : 0; }
+
+void r2p_batch_destroy(r2p_batch* b)
+{
+    if (!b) return;
+    cudaSetDevice(b->eng->device);
+    cudaDeviceSynchronize();
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->mem) cudaFree(b->mem);
+    delete b;
 }
 
 uint32_t r2p_crc32_combine(uint32_t crc1, uint32_t crc2, uint64_t len2)

@@ -32,6 +32,6 @@ cudaError_t launch_checksum(const uint8_t* data, uint64_t len, bool adler, uint3
 // k_lz77.cu
 uint64_t lz77_slot_bytes(int block_size);
 cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
-                        uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s);
+                        uint64_t slot_bytes, const uint32_t* xpow, int grid, int hash_bits, cudaStream_t s);
 
 }  // namespace r2p

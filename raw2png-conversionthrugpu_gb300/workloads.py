@@ -134,3 +134,30 @@ def image_ct8(width, height, wc, ww, level=1):
 def image_ct16(width, height, wc, ww, level=1):
     p = DicomParams.make(16, 12, 11, 0, slope=1.0, intercept=-1024.0, wc=wc, ww=ww)
     return Image.make(width, height, 1, 2, WINDOW_DICOM16, p, level=level, strip_height=1024)
+
+
+def ct_phantom_torch(seed, width, height, device="cuda", noise=20.0):
+    """ct_phantom's recipe drawn on the GPU with torch (same distributions,
+    torch's generator): returns an int16 device tensor of LE 12-bit values."""
+    import torch
+    rng = np.random.default_rng(seed)
+    cy, cx = height / 2.0, width / 2.0
+    ry, rx = 0.40 * height, 0.44 * width
+    y = torch.arange(height, device=device, dtype=torch.float32)[:, None]
+    x = torch.arange(width, device=device, dtype=torch.float32)[None, :]
+
+    def ell(ey, ex, ay, ax):
+        return ((y - ey) / ay) ** 2 + ((x - ex) / ax) ** 2 <= 1.0
+
+    img = torch.zeros((height, width), device=device, dtype=torch.float32)
+    img[ell(cy, cx, ry, rx)] = 1064.0
+    for _ in range(6):
+        ey = cy + rng.uniform(-0.5, 0.5) * ry
+        ex = cx + rng.uniform(-0.5, 0.5) * rx
+        ay = rng.uniform(0.05, 0.25) * ry
+        ax = rng.uniform(0.05, 0.25) * rx
+        img[ell(ey, ex, ay, ax)] = float(rng.uniform(900.0, 2200.0))
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    img += torch.randn((height, width), device=device, generator=g) * noise
+    return torch.clamp(torch.round(img), 0, 4095).to(torch.int16)

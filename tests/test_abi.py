@@ -42,6 +42,9 @@ def test_host_crc_and_adler_combine(r2p):
 
 def test_png_bound_and_validation(r2p, W):
     img = W.image_c0()
+    nb = -(-img.filtered_bytes // 1024)
+    assert r2p.png_bound(img) == 43 + img.filtered_bytes + 5 * nb + 20
+    img.block_size = r2p.BLOCK64
     assert r2p.png_bound(img) == 43 + img.filtered_bytes + 5 * 5 + 20
     bad = W.image_c0()
     bad.channels = 2

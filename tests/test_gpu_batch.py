@@ -1,0 +1,73 @@
+"""Batched encoding: one planned work list over many images, launched
+directly or replayed as a CUDA graph, and size-class tuning.
+
+Every PNG is decoded by the oracle's reader and compared with the oracle's
+pixels and filtered scanlines (see test_gpu_png.decode_and_check); graph
+replays and direct launches must give byte-identical files.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_png import decode_and_check
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch_inputs(r2p, W, specs, level=1):
+    imgs, raws, bufs, outs, caps = [], [], [], [], []
+    for i, (w, h, wc, ww) in enumerate(specs):
+        raw = W.ct_phantom(100 + i, w, h)
+        img = W.image_ct8(w, h, wc, ww, level=level)
+        imgs.append(img)
+        raws.append(raw)
+        bufs.append(r2p.DeviceBuffer.from_array(raw))
+        caps.append(r2p.png_bound(img))
+        outs.append(r2p.DeviceBuffer(caps[-1]))
+    lens = r2p.DeviceBuffer(8 * len(imgs))
+    return imgs, raws, bufs, outs, caps, lens
+
+
+def read_all(outs, lens, n):
+    ln = lens.download(8 * n).view(np.uint64)
+    return [outs[i].download(int(ln[i])).tobytes() for i in range(n)]
+
+
+SPECS = [(256, 256, 40.0, 400.0), (512, 512, -300.0, 1500.0), (1024, 64, 100.0, 90.0), (33, 7, 0.0, 800.0),
+         (700, 300, -600.0, 250.0), (256, 256, 350.0, 1200.0)]
+
+
+def test_batch_direct_and_graph(engine, O, r2p, W):
+    imgs, raws, bufs, outs, caps, lens = make_batch_inputs(r2p, W, SPECS)
+    b = engine.batch(imgs, [x.ptr for x in bufs], [o.ptr for o in outs], caps, lens.ptr)
+    assert b.device_bytes > 0
+    b.launch()
+    direct = read_all(outs, lens, len(imgs))
+    for i in range(len(imgs)):
+        decode_and_check(O, r2p, imgs[i], raws[i], direct[i])
+    for _ in range(2):
+        for o in outs:
+            o.memset(0)
+        b.launch_graph()
+        assert read_all(outs, lens, len(imgs)) == direct
+    b.close()
+    # the same images one call each give the same files
+    for i in range(len(imgs)):
+        assert engine.encode_png(imgs[i], raws[i]) == direct[i]
+
+
+def test_tuning_table_changes_blocks_not_pixels(O, r2p, W):
+    eng = r2p.Engine(0)
+    eng.set_tuning([(300000, 4096, 8, 10), (2 ** 40, 32752, 0, 11)])
+    assert eng.get_tuning()[0] == (300000, 4096, 8, 10)
+    imgs, raws, bufs, outs, caps, lens = make_batch_inputs(r2p, W, SPECS)
+    b = eng.batch(imgs, [x.ptr for x in bufs], [o.ptr for o in outs], caps, lens.ptr)
+    b.launch_graph()
+    pngs = read_all(outs, lens, len(imgs))
+    for i in range(len(imgs)):
+        decode_and_check(O, r2p, imgs[i], raws[i], pngs[i])
+    b.close()
+    with pytest.raises(r2p.R2PError):
+        eng.set_tuning([(100, 4096, 0, 12)])
+    eng.set_tuning([])
+    assert eng.get_tuning()[0][1] == r2p.BLOCK64
+    eng.close()

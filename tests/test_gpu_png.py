@@ -36,7 +36,7 @@ def test_c0_png_stored(engine, O, r2p, W):
     png = engine.encode_png(img, raw)
     decode_and_check(O, r2p, img, raw, png)
     assert len(png) <= r2p.png_bound(img)
-    # level 0 stores every filtered byte: 262,656 bytes in 5 stored blocks
+    # level 0 stores every filtered byte: 262,656 bytes in 5 stored blocks of 65520
     assert len(png) == 43 + img.filtered_bytes + 5 * 5 + 20
 
 
