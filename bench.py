@@ -209,6 +209,105 @@ def measure_c3(r2p, W, eng, stream, n=1000, reps=3):
     return res
 
 
+def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4, threads=4):
+    """Served request stream: Poisson arrivals at fractions of the measured
+    saturation rate; p50/p99 latency (submit -> PNG in host memory) and images/s,
+    next to the plain per-image path (r2p_encode_png, one image at a time)."""
+    import random
+    import threading
+    specs = W.request_specs(n_pool, seed)
+    import ctypes
+    pool = []
+    for (w, h, eight, wc, ww, sd) in specs:
+        raw = W.ct_phantom_torch(sd, w, h).cpu().numpy().view(np.uint8).reshape(-1)
+        img = W.image_ct8(w, h, wc, ww, level=1) if eight else W.image_ct16(w, h, wc, ww, level=1)
+        pin = r2p.PinnedBuffer(img.raw_bytes)     # requests arrive in pinned host memory
+        pin.array[:] = raw
+        pool.append((img, pin))
+    mean_raw = sum(im.raw_bytes for im, _ in pool) / len(pool)
+    # plain per-image path on the same GPU: r2p_encode_png from the same pinned
+    # buffers into a pinned PNG buffer, one image at a time
+    eng = r2p.Engine(0)
+    load_tuning(eng)
+    out = r2p.PinnedBuffer(max(r2p.png_bound(im) for im, _ in pool))
+    n = ctypes.c_size_t()
+
+    def plain(img, pin):
+        r2p.check(r2p.lib().r2p_encode_png(eng.h, ctypes.byref(img), pin.ptr, out.ptr, out.nbytes, ctypes.byref(n)))
+
+    for img, pin in pool[:4]:
+        plain(img, pin)
+    t0 = time.perf_counter()
+    for img, pin in pool:
+        plain(img, pin)
+    plain_ips = len(pool) / (time.perf_counter() - t0)
+    eng.close()
+    sv = r2p.Server(0, hbm_budget=40 << 30, host_pool_bytes=8 << 30, max_inflight_batches=3)
+    try:
+        with open(TUNING_JSON) as f:
+            sv.set_tuning([tuple(c) for c in json.load(f)["classes"]])
+    except (OSError, KeyError, ValueError):
+        pass
+
+    def run(arrivals):
+        """Submit request k at time arrivals[k] (seconds from start) from
+        `threads` submitters; return (latencies ms, wall seconds)."""
+        n = len(arrivals)
+        tickets = [None] * n
+        start = time.perf_counter() + 0.02
+
+        def submitter(k):
+            for i in range(k, n, threads):
+                dt = start + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                img, pin = pool[i % len(pool)]
+                tickets[i] = sv.submit(img, pin, borrow=True)
+
+        ths = [threading.Thread(target=submitter, args=(k,)) for k in range(threads)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        lat = []
+        for t in tickets:
+            st, png_len, l, q = sv.wait(t, timeout_ms=120000, fetch=False)
+            if st != r2p.OK or not png_len:
+                raise RuntimeError(f"served request {t} ended with status {st}")
+            lat.append(l)
+        wall = time.perf_counter() - start
+        return lat, wall
+
+    # saturation: everything arrives at once
+    run([0.0] * 64)
+    sv.reset_stats()
+    lat, wall = run([0.0] * per_level)
+    sat = per_level / wall
+    st = sv.stats()
+    out = {"requests_per_level": per_level, "pool_images": len(pool), "mean_raw_bytes": int(mean_raw),
+           "plain_images_per_s": round(plain_ips, 1), "saturation_images_per_s": round(sat, 1),
+           "saturation_vs_plain": round(sat / plain_ips, 2), "mean_batch_images_at_saturation":
+           round(st["mean_batch_images"], 1), "levels": []}
+    rng = random.Random(seed)
+    for f in levels:
+        lam = f * sat
+        t, arr = 0.0, []
+        for _ in range(per_level):
+            t += rng.expovariate(lam)
+            arr.append(t)
+        sv.reset_stats()
+        lat, wall = run(arr)
+        lat.sort()
+        st = sv.stats()
+        out["levels"].append({"load": f, "offered_images_per_s": round(lam, 1),
+                              "achieved_images_per_s": round(per_level / wall, 1),
+                              "p50_ms": round(lat[len(lat) // 2], 3),
+                              "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))], 3),
+                              "mean_batch_images": round(st["mean_batch_images"], 2)})
+    sv.close()
+    return out
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -418,6 +517,7 @@ def run_ours(args):
     line["config"]["tuning"] = tuning
     if not args.no_batched:
         line["batched_c3"] = measure_c3(r2p, W, eng, stream)
+        line["served_c4"] = measure_c4(r2p, W)
     if world == 1 and not args.no_cpu_baseline:
         from oracle import build_oracle, oracle as O
         build_oracle.build_oracle()
@@ -449,7 +549,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c3"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c3", "c4"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
@@ -459,6 +559,12 @@ def main():
         run_reference(args)
     elif args.workload == "c3":
         run_c3(args)
+    elif args.workload == "c4":
+        import __graft_entry__ as g
+        r2p = g.load_package()
+        from raw2png_gb300 import workloads as W
+        print(json.dumps({"metric": "served images/s and p50/p99 latency", "served_c4": measure_c4(r2p, W)}),
+              flush=True)
     else:
         run_ours(args)
 

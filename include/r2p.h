@@ -182,6 +182,55 @@ size_t r2p_zlib_bound(size_t len, int level, int block_size);
 int r2p_zlib_compress_noalloc(const void* d_in, size_t len, int level, int block_size,
                               void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream);
 
+/* ---- serving: continuous batching ------------------------------------- */
+/* A server owns a device (an engine), a pooled device arena of hbm_budget
+ * bytes and a pinned host pool.  Requests are admitted against the budget;
+ * a dispatcher thread launches a batch of pending requests whenever one of
+ * max_inflight_batches stream slots is free, so requests that arrive while
+ * others run join the next batch and batches overlap on the device.  Results
+ * come back to host memory owned by the server until r2p_server_release.
+ * Replaces the reference's per-file worker pools and queues
+ * (src/batch_processor.cpp:482-737, src/pipeline.cpp:445-1291). */
+typedef struct r2p_server r2p_server;
+typedef struct r2p_server_config {
+    size_t hbm_budget;            /* device bytes for requests + scratch (0 = 40 GiB) */
+    size_t host_pool_bytes;       /* pinned host bytes for pixels + PNGs (0 = 4 GiB) */
+    int    max_inflight_batches;  /* concurrent batches / streams (0 = 3) */
+    int    max_batch_images;      /* requests per batch at most (0 = 512) */
+} r2p_server_config;
+typedef struct r2p_result {
+    int            status;        /* R2P_OK, R2P_ECANCELED, or the failure */
+    const uint8_t* png;           /* server-owned until r2p_server_release */
+    size_t         png_len;
+    double         latency_ms;    /* submit -> PNG in host memory */
+    double         queue_ms;      /* submit -> dispatched in a batch */
+} r2p_result;
+typedef struct r2p_server_stats {
+    uint64_t completed, failed, canceled, batches, pending;
+    double   mean_batch_images;
+    double   p50_ms, p99_ms, max_ms;
+    size_t   device_bytes_in_use, device_bytes_peak;
+} r2p_server_stats;
+int  r2p_server_create(int device, const r2p_server_config* cfg, r2p_server** out);
+int  r2p_server_set_tuning(r2p_server* srv, int n, const r2p_tuning* classes);
+/* Copies the pixels; R2P_EBUDGET if the request can never fit the budget. */
+int  r2p_server_submit(r2p_server* srv, const r2p_image* img, const void* h_pixels, uint64_t* ticket);
+/* flags R2P_SUBMIT_BORROW: no copy -- the server reads h_pixels directly (best
+ * from pinned memory), which must stay valid and unchanged until the request's
+ * wait returns or it is cancelled. */
+#define R2P_SUBMIT_BORROW 1u
+int  r2p_server_submit_ex(r2p_server* srv, const r2p_image* img, const void* h_pixels, uint32_t flags,
+                          uint64_t* ticket);
+/* timeout_ms < 0 waits without limit; R2P_ETIMEOUT if still running. */
+int  r2p_server_wait(r2p_server* srv, uint64_t ticket, int timeout_ms, r2p_result* res);
+/* Only requests not yet dispatched can be cancelled. */
+int  r2p_server_cancel(r2p_server* srv, uint64_t ticket);
+int  r2p_server_release(r2p_server* srv, uint64_t ticket);
+int  r2p_server_get_stats(r2p_server* srv, r2p_server_stats* st);
+int  r2p_server_reset_stats(r2p_server* srv);
+/* Drains in-flight work, then frees everything. */
+void r2p_server_destroy(r2p_server* srv);
+
 /* ---- checksums (device data) ------------------------------------------- */
 /* Replace gpu_adler32_compute (include/gpu_adler32.h:25) and
  * gpu_crc32_compute (include/gpu_crc32.h:29); results land in *d_result (a

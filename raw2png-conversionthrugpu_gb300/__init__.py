@@ -74,6 +74,23 @@ class Tuning(ctypes.Structure):
                 ("hash_bits", ctypes.c_int)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_size_t), ("host_pool_bytes", ctypes.c_size_t),
+                ("max_inflight_batches", ctypes.c_int), ("max_batch_images", ctypes.c_int)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("png", ctypes.POINTER(ctypes.c_uint8)), ("png_len", ctypes.c_size_t),
+                ("latency_ms", ctypes.c_double), ("queue_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("canceled", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("pending", ctypes.c_uint64), ("mean_batch_images", ctypes.c_double),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("device_bytes_in_use", ctypes.c_size_t), ("device_bytes_peak", ctypes.c_size_t)]
+
+
 class Image(ctypes.Structure):
     """r2p_image."""
     _fields_ = [
@@ -162,6 +179,16 @@ SIGNATURES = {
     "r2p_batch_device_bytes": (_sz, [_vp]),
     "r2p_batch_destroy": (None, [_vp]),
     "r2p_engine_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Tuning)]),
+    "r2p_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
+    "r2p_server_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Tuning)]),
+    "r2p_server_submit": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _u64p]),
+    "r2p_server_submit_ex": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, ctypes.c_uint32, _u64p]),
+    "r2p_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(Result)]),
+    "r2p_server_cancel": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+    "r2p_server_release": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+    "r2p_server_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    "r2p_server_reset_stats": (ctypes.c_int, [_vp]),
+    "r2p_server_destroy": (None, [_vp]),
     "r2p_engine_get_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_int)]),
     "r2p_engine_stage_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _u64p]),
 }
@@ -459,6 +486,74 @@ class Batch:
         if getattr(self, "h", None):
             lib().r2p_batch_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request server (r2p_server)."""
+
+    def __init__(self, device=0, hbm_budget=0, host_pool_bytes=0, max_inflight_batches=0, max_batch_images=0):
+        cfg = ServerConfig(hbm_budget, host_pool_bytes, max_inflight_batches, max_batch_images)
+        p = _vp()
+        check(lib().r2p_server_create(device, ctypes.byref(cfg), ctypes.byref(p)))
+        self.h = p.value
+
+    def set_tuning(self, classes):
+        arr = (Tuning * len(classes))(*[Tuning(*c) for c in classes]) if classes else None
+        check(lib().r2p_server_set_tuning(self.h, len(classes), arr))
+
+    def submit(self, img, pixels, borrow=False):
+        """Queue one image.  borrow=True: no copy; `pixels` (a numpy array or
+        a PinnedBuffer) must stay alive and unchanged until wait() returns."""
+        if isinstance(pixels, PinnedBuffer):
+            ptr, nbytes = pixels.ptr, pixels.nbytes
+        else:
+            px = np.ascontiguousarray(pixels).view(np.uint8).reshape(-1)
+            ptr, nbytes = px.ctypes.data, px.nbytes
+        assert nbytes >= img.raw_bytes
+        t = ctypes.c_uint64()
+        check(lib().r2p_server_submit_ex(self.h, ctypes.byref(img), ptr, 1 if borrow else 0, ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1, release=True, fetch=True):
+        """(status, png bytes (or its length when fetch=False) or None, latency_ms, queue_ms)."""
+        r = Result()
+        st = lib().r2p_server_wait(self.h, ticket, timeout_ms, ctypes.byref(r))
+        if st == ETIMEOUT:
+            return ETIMEOUT, None, None, None
+        png = None
+        if st == OK and r.png_len:
+            png = ctypes.string_at(r.png, r.png_len) if fetch else r.png_len
+        if release:
+            lib().r2p_server_release(self.h, ticket)
+        return st, png, r.latency_ms, r.queue_ms
+
+    def cancel(self, ticket):
+        return lib().r2p_server_cancel(self.h, ticket)
+
+    def stats(self):
+        st = ServerStats()
+        check(lib().r2p_server_get_stats(self.h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def reset_stats(self):
+        check(lib().r2p_server_reset_stats(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().r2p_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def __del__(self):
         try:
