@@ -155,6 +155,14 @@ int r2p_engine_get_tuning(r2p_engine* eng, int cap, r2p_tuning* out, int* n);
  * gpu_filter_process_from_device (include/gpu_filter.h:41-47). */
 int r2p_window_filter_device(r2p_engine* eng, const r2p_image* img, const void* d_pixels,
                              const void* d_prior, void* d_filtered, void* stream);
+/* As above; d_last_row (may be NULL) also receives the image's last row
+ * after windowing (row_bytes bytes, PNG byte order): the row above the next
+ * strip.  Replaces the carry that gpu_filter_process_* keeps between strips
+ * and gpu_filter_copy_prior_row_to_host reads (src/gpu_filter.cu:428-434,
+ * include/gpu_filter.h:76-90). */
+int r2p_window_filter_device_ex(r2p_engine* eng, const r2p_image* img, const void* d_pixels,
+                                const void* d_prior, void* d_filtered, void* d_last_row,
+                                void* stream);
 
 /* Stage entry point: zlib stream (header, DEFLATE blocks, Adler-32 trailer)
  * of already-filtered bytes, on the device.  Replaces gpu_deflate_compress_strip
@@ -164,6 +172,18 @@ int r2p_zlib_compress_device(r2p_engine* eng, const void* d_in, size_t len, int 
                              int block_size, void* d_out, size_t out_cap,
                              uint64_t* d_out_len, void* stream);
 size_t r2p_zlib_bound(size_t len, int level, int block_size);
+
+/* Raw DEFLATE (no zlib header or trailer) of one part of a longer stream:
+ * the strip contract of CompressionBackend::compress_strip
+ * (include/compression_backend.h:33-43, src/parallel_deflate.cpp:141-170).
+ * final_part = 0 leaves the stream open: no block has BFINAL set and the
+ * part ends byte-aligned on an empty stored block, so parts concatenate into
+ * one valid stream; final_part = 1 sets BFINAL on the last block.  The
+ * input's Adler-32 follows the *d_out_len stream bytes as 4 big-endian bytes
+ * (not counted).  out_cap >= r2p_zlib_bound(len, level, block_size). */
+int r2p_deflate_raw_device(r2p_engine* eng, const void* d_in, size_t len, int level,
+                           int block_size, int final_part, void* d_out, size_t out_cap,
+                           uint64_t* d_out_len, void* stream);
 
 /* Allocation-free form of r2p_zlib_compress_device, for callers that cannot
  * allocate device memory once running: code hosted in a framework that owns

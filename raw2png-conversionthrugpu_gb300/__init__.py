@@ -150,8 +150,11 @@ SIGNATURES = {
     "r2p_encode_batch_device": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Image), ctypes.POINTER(_vp),
                                                ctypes.POINTER(_vp), ctypes.POINTER(_sz), _vp, _vp]),
     "r2p_window_filter_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp]),
+    "r2p_window_filter_device_ex": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp, _vp]),
     "r2p_zlib_compress_device": (ctypes.c_int, [_vp, _vp, _sz, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _vp]),
     "r2p_zlib_bound": (_sz, [_sz, ctypes.c_int, ctypes.c_int]),
+    "r2p_deflate_raw_device": (ctypes.c_int, [_vp, _vp, _sz, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp,
+                                              _vp]),
     "r2p_zlib_compress_noalloc": (ctypes.c_int, [_vp, _sz, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _vp]),
     "r2p_adler32_device": (ctypes.c_int, [_vp, _vp, _sz, _vp, _vp]),
     "r2p_crc32_device": (ctypes.c_int, [_vp, _vp, _sz, _vp, _vp]),
@@ -394,8 +397,9 @@ class Engine:
         cp = (_sz * n)(*caps)
         check(lib().r2p_encode_batch_device(self.h, n, arr, px, pg, cp, d_lens, _sp(stream)))
 
-    def window_filter_device(self, img, d_pixels, d_filtered, d_prior=None, stream=None):
-        check(lib().r2p_window_filter_device(self.h, ctypes.byref(img), d_pixels, d_prior, d_filtered, _sp(stream)))
+    def window_filter_device(self, img, d_pixels, d_filtered, d_prior=None, stream=None, d_last_row=None):
+        check(lib().r2p_window_filter_device_ex(self.h, ctypes.byref(img), d_pixels, d_prior, d_filtered, d_last_row,
+                                                _sp(stream)))
 
     def zlib_compress_device(self, d_in, n, level, d_out, out_cap, d_len, block_size=0, stream=None):
         check(lib().r2p_zlib_compress_device(self.h, d_in, n, level, block_size, d_out, out_cap, d_len, _sp(stream)))
@@ -449,6 +453,21 @@ class Engine:
         if n >> 63:
             raise R2PError(n & 0xFF, "device reported an error")
         return dst.download(n).tobytes()
+
+    def deflate_raw(self, data, level, final_part, block_size=0):
+        """Raw DEFLATE of one stream part: (stream bytes, Adler-32 of data)."""
+        data = np.ascontiguousarray(data, np.uint8).reshape(-1)
+        src = DeviceBuffer.from_array(data)
+        cap = zlib_bound(data.size, level, block_size)
+        dst = DeviceBuffer(cap)
+        ln = DeviceBuffer(8)
+        check(lib().r2p_deflate_raw_device(self.h, src.ptr, data.size, level, block_size, 1 if final_part else 0,
+                                           dst.ptr, cap, ln.ptr, None))
+        n = int(ln.download(8).view(np.uint64)[0])
+        if n >> 63:
+            raise R2PError(n & 0xFF, "device reported an error")
+        out = dst.download(n + 4).tobytes()
+        return out[:n], int.from_bytes(out[n:], "big")
 
     def checksum(self, data, kind):
         data = np.ascontiguousarray(data, np.uint8).reshape(-1)

@@ -52,19 +52,68 @@ def _compile(src, verbose):
     return obj
 
 
+# C++17 host layer: the reference's C++ interfaces (gpu_filter.h,
+# compression_backend.h, pipeline.h, DicomSource, PngWriter) over the C ABI,
+# and the gpu_png_encoder command line.  No CUDA headers: it links libr2p.so.
+HOST = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(HERE, "libr2p_host.so")
+CLI = os.path.join(HERE, "gpu_png_encoder")
+HOST_SOURCES = ["gpu_filter.cpp", "compression_backend.cpp", "parallel_deflate.cpp", "png_writer.cpp",
+                "file_type.cpp", "dicom_loader.cpp", "pipeline.cpp", "batch_processor.cpp"]
+CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter", "-ffp-contract=off",
+             "-I" + os.path.join(HOST, "include"), "-I" + INCLUDE]
+
+
+def cxx():
+    return shutil.which("g++") or "g++"
+
+
+def _host_headers():
+    d = [os.path.join(HOST, "include"), os.path.join(HOST, "src")]
+    return [os.path.join(x, f) for x in d for f in os.listdir(x) if f.endswith(".h")] + \
+        [os.path.join(INCLUDE, "r2p.h")]
+
+
+def _compile_host(src, verbose):
+    obj = os.path.join(BUILD, "host_" + os.path.basename(src) + ".o")
+    if not _stale(obj, [src, __file__] + _host_headers()):
+        return obj
+    cmd = [cxx()] + CXX_FLAGS + ["-c", src, "-o", obj + ".tmp"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+    os.replace(obj + ".tmp", obj)
+    return obj
+
+
+def _link(out, cmd, deps, verbose):
+    if not _stale(out, deps):
+        return
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link of %s failed:\n%s%s" % (os.path.basename(out), r.stdout, r.stderr))
+    os.replace(out + ".tmp", out)
+
+
 def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(CSRC, f) for f in CU_SOURCES]
-    with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lpthread"]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
-        os.replace(LIB + ".tmp", LIB)
+    hsrcs = [os.path.join(HOST, "src", f) for f in HOST_SOURCES + ["main.cpp"]]
+    with cf.ThreadPoolExecutor(max_workers=len(srcs) + len(hsrcs)) as ex:
+        fo = [ex.submit(_compile, s, verbose) for s in srcs]
+        fh = [ex.submit(_compile_host, s, verbose) for s in hsrcs]
+        objs = [f.result() for f in fo]
+        hobjs = [f.result() for f in fh]
+    _link(LIB, [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lpthread"], objs, verbose)
+    rpath = ["-Wl,-rpath,$ORIGIN", "-L" + HERE]
+    _link(HOST_LIB, [cxx(), "-shared", "-o", HOST_LIB + ".tmp"] + hobjs[:-1] + rpath + ["-lr2p", "-lpthread"],
+          hobjs[:-1] + [LIB], verbose)
+    _link(CLI, [cxx(), "-o", CLI + ".tmp", hobjs[-1]] + rpath + ["-lr2p_host", "-lr2p", "-lpthread"],
+          [hobjs[-1], HOST_LIB, LIB], verbose)
     return LIB
 
 

@@ -51,7 +51,7 @@ k_stored_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks
         }
         __syncthreads();
         const int local = (int)(b - d.blk0);
-        const bool last = (local == d.nblocks - 1);
+        const bool last = (local == d.nblocks - 1) && !d.open_end;
         uint8_t* dst = d.png + d.prefix + (size_t)local * (size_t)(kStoredHdr + d.block_size);
         uint8_t hdr[kStoredHdr] = {(uint8_t)(last ? 1 : 0), (uint8_t)(n & 0xFF), (uint8_t)(n >> 8),
                                    (uint8_t)(~n & 0xFF), (uint8_t)((~n >> 8) & 0xFF)};
@@ -155,9 +155,10 @@ k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uin
     s2 = cta_sum64<kFinThreads>(s2, red64);
     cx = cta_xor<kFinThreads>(cx, red32);
     if (threadIdx.x == 0) {
-        const bool png = (d.out_kind == 0);
-        const uint64_t total = png ? (uint64_t)kPngPrefix + Ls + kPngSuffix : 2 + Ls + 4;
-        if (d.status == 0 && total > d.png_cap) d.status = R2P_ENOSPC;
+        const bool png = (d.out_kind == 0), raw = (d.out_kind == 2);
+        // raw DEFLATE: the input's Adler-32 follows the stream (4 bytes, big-endian, not counted)
+        const uint64_t total = png ? (uint64_t)kPngPrefix + Ls + kPngSuffix : raw ? Ls : 2 + Ls + 4;
+        if (d.status == 0 && total + (raw ? 4 : 0) > d.png_cap) d.status = R2P_ENOSPC;
         if (d.status) {                    // error word: top bit set, status in the low bits
             *d.png_len = (1ull << 63) | (uint64_t)d.status;
             return;
@@ -170,6 +171,10 @@ k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uin
         put_be32(trl, adler);
         uint8_t* q = p + d.prefix + Ls;
         for (int i = 0; i < 4; i++) q[i] = trl[i];
+        if (raw) {
+            *d.png_len = total;
+            return;
+        }
         if (!png) {
             p[0] = head[4];
             p[1] = head[5];

@@ -614,6 +614,9 @@ k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items,
                 if (!active) continue;
                 const int f = best_filter(s);
                 const int r = t0 + j;
+                if (d.last_row && r == (int)d.height - 1) {   // the next strip's row above
+                    for (int i = wg * 32 + lane; i < rb; i += 32 * G) d.last_row[i] = xr[i];
+                }
                 uint8_t* orow = d.filt + (size_t)r * (size_t)(rb + 1);
                 const uintptr_t data_addr = reinterpret_cast<uintptr_t>(orow + 1);
                 const int e = (int)(data_addr & 3);

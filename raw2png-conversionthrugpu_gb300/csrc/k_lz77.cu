@@ -220,7 +220,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         if (d.level == 0) continue;
         const int n = (int)bo.in_len;
         const uint8_t* src = d.filt + bo.in_off;
-        const bool last = ((int)(b - d.blk0) == d.nblocks - 1);
+        const bool last = ((int)(b - d.blk0) == d.nblocks - 1) && !d.open_end;
         __syncthreads();
         // stage the block (+ zero padding), clear the hash tables
         if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {

@@ -42,12 +42,14 @@ struct DevImage {
     const uint8_t* raw;
     uint8_t* filt;
     const uint8_t* prior;           // windowed row above row 0 (rb bytes) or null
+    uint8_t* last_row;              // receives the windowed last row (rb bytes) or null
     // DEFLATE / PNG
     int32_t level;
     int32_t block_size;             // filtered bytes per DEFLATE block
     int32_t nblocks;
     uint32_t blk0;                  // first global block index of this image
-    int32_t out_kind;               // 0 = PNG file, 1 = bare zlib stream
+    int32_t out_kind;               // 0 = PNG file, 1 = bare zlib stream, 2 = raw DEFLATE
+    int32_t open_end;               // 1: no BFINAL; the last block ends with an empty stored block
     int32_t prefix;                 // bytes before the DEFLATE stream (kPngPrefix or 2)
     uint8_t* png;                   // output buffer
     uint64_t png_cap;

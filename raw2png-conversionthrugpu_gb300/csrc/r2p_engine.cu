@@ -166,7 +166,7 @@ static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip,
     const uint64_t nb = (F + bs - 1) / bs;
     d.nblocks = (int32_t)nb;
     d.out_kind = out_kind;
-    d.prefix = out_kind == 0 ? kPngPrefix : 2;
+    d.prefix = out_kind == 0 ? kPngPrefix : out_kind == 1 ? 2 : 0;
     ip.raw_bytes = pitch * im.height;
     // worst-case table for the window request (resolved on the device)
     int entries = 0, esize = 0, mode_guess = W_COPY;
@@ -238,6 +238,7 @@ struct CallBuffers {
     std::vector<const uint8_t*> raw;
     std::vector<uint8_t*> filt;
     std::vector<const uint8_t*> prior;
+    std::vector<uint8_t*> last_row;     // optional; empty = none
     std::vector<uint8_t*> out;
     std::vector<uint64_t> out_cap;
     std::vector<uint64_t*> out_len;
@@ -360,6 +361,7 @@ static void fill_pointers(std::vector<ImgPlan>& plans, const CallBuffers& cb, co
         lut_off += plans[i].lut_cap;
         d.raw = cb.raw[i];
         d.prior = cb.prior[i];
+        d.last_row = i < cb.last_row.size() ? cb.last_row[i] : nullptr;
         if (cb.filt[i]) {
             d.filt = cb.filt[i];
         } else {
@@ -689,6 +691,12 @@ int r2p_encode_png(r2p_engine* e, const r2p_image* img, const void* h_pixels, vo
 int r2p_window_filter_device(r2p_engine* e, const r2p_image* img, const void* d_pixels, const void* d_prior,
                              void* d_filtered, void* stream)
 {
+    return r2p_window_filter_device_ex(e, img, d_pixels, d_prior, d_filtered, nullptr, stream);
+}
+
+int r2p_window_filter_device_ex(r2p_engine* e, const r2p_image* img, const void* d_pixels, const void* d_prior,
+                                void* d_filtered, void* d_last_row, void* stream)
+{
     if (!e || !img || !d_pixels || !d_filtered) return set_err(R2P_EINVAL, "NULL argument");
     std::lock_guard<std::mutex> lk(e->mu);
     int rc = bind(e);
@@ -700,14 +708,32 @@ int r2p_window_filter_device(r2p_engine* e, const r2p_image* img, const void* d_
     cb.raw = {static_cast<const uint8_t*>(d_pixels)};
     cb.filt = {static_cast<uint8_t*>(d_filtered)};
     cb.prior = {static_cast<const uint8_t*>(d_prior)};
+    cb.last_row = {static_cast<uint8_t*>(d_last_row)};
     cb.out = {nullptr};
     cb.out_cap = {0};
     cb.out_len = {nullptr};
     return run(e, plans, cb, ST_FILTER, static_cast<cudaStream_t>(stream));
 }
 
+// One DEFLATE stream over device bytes: a zlib stream (out_kind 1) or raw
+// DEFLATE (out_kind 2, optionally left open for a following stream part).
+static int deflate_bytes(r2p_engine* e, const void* d_in, size_t len, int level, int block_size, int out_kind,
+                         int open_end, void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream);
+
 int r2p_zlib_compress_device(r2p_engine* e, const void* d_in, size_t len, int level, int block_size,
                              void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream)
+{
+    return deflate_bytes(e, d_in, len, level, block_size, 1, 0, d_out, out_cap, d_out_len, stream);
+}
+
+int r2p_deflate_raw_device(r2p_engine* e, const void* d_in, size_t len, int level, int block_size, int final_part,
+                           void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream)
+{
+    return deflate_bytes(e, d_in, len, level, block_size, 2, final_part ? 0 : 1, d_out, out_cap, d_out_len, stream);
+}
+
+static int deflate_bytes(r2p_engine* e, const void* d_in, size_t len, int level, int block_size, int out_kind,
+                         int open_end, void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream)
 {
     if (!e || !d_in || !d_out || !d_out_len) return set_err(R2P_EINVAL, "NULL argument");
     if (len == 0 || len >= (1ull << 31)) return set_err(R2P_EINVAL, "len must be in [1, 2^31)");
@@ -728,8 +754,9 @@ int r2p_zlib_compress_device(r2p_engine* e, const void* d_in, size_t len, int le
     d.level = level;
     d.block_size = bs;
     d.nblocks = (int32_t)((len + bs - 1) / bs);
-    d.out_kind = 1;
-    d.prefix = 2;
+    d.out_kind = out_kind;
+    d.open_end = open_end;
+    d.prefix = out_kind == 1 ? 2 : 0;
     d.req_mode = R2P_WINDOW_NONE;
     plans[0].smem = 0;
     plans[0].lreg = 0;

@@ -88,3 +88,30 @@ def test_deterministic_output(engine, W, r2p):
     a = engine.encode_png(img, raw)
     b = engine.encode_png(img, raw)
     assert a == b
+
+
+@pytest.mark.parametrize("level", [0, 1])
+def test_raw_deflate_parts_concatenate(engine, level):
+    """r2p_deflate_raw_device: open parts (no BFINAL, byte-aligned end) and a
+    final part concatenate into one raw DEFLATE stream that stock zlib
+    inflates to the input, each part reporting its own Adler-32 -- the
+    compress_strip contract (include/compression_backend.h:33-43)."""
+    rng = np.random.default_rng(77 + level)
+    sizes = [70001, 1, 65520, 200000, 4097]
+    pieces = []
+    for i, n in enumerate(sizes):
+        base = rng.integers(0, 6, size=n, dtype=np.uint8)
+        base[::7] = rng.integers(0, 256, size=base[::7].size, dtype=np.uint8)
+        pieces.append(base)
+    stream, total = b"", b""
+    for i, p in enumerate(pieces):
+        last = i == len(pieces) - 1
+        part, adler = engine.deflate_raw(p, level, last)
+        assert adler == zlib.adler32(p.tobytes())
+        d = zlib.decompressobj(-15)
+        assert d.decompress(part) == p.tobytes()
+        assert d.eof == last, "only the final part may end the stream"
+        stream += part
+        total += p.tobytes()
+    d = zlib.decompressobj(-15)
+    assert d.decompress(stream) == total and d.eof and d.unused_data == b""

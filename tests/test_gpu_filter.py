@@ -174,3 +174,40 @@ def test_random_fuzz(engine, O, r2p):
             img = r2p.Image.make(w, h, ch, bps, mode)
             raw = rng.integers(0, 256, size=w * h * ch * bps, dtype=np.uint8)
         check(engine, O, r2p, img, raw)
+
+
+@pytest.mark.parametrize("mode", ["a2", "batch8", "none_rgb16"])
+def test_strips_with_carried_last_row(engine, O, r2p, W, mode):
+    """Strip-by-strip filtering with the windowed last row carried between
+    strips (r2p_window_filter_device_ex) equals filtering the whole image, as
+    the reference's per-strip prior-row carry does (src/gpu_filter.cu:428-434)."""
+    w, h, strip = 257, 203, 64
+    if mode == "a2":
+        raw = W.radial_rects(4, w, h)
+        full = r2p.Image.make(w, h, 1, 2, r2p.WINDOW_DICOM16, r2p.DicomParams.make(16, 12, 11, 0, wc=1500.0,
+                                                                                   ww=3000.0))
+    elif mode == "batch8":
+        raw = W.ct_phantom(4, w, h)
+        full = W.image_ct8(w, h, 40.0, 400.0)
+    else:
+        raw = np.random.default_rng(4).integers(0, 65536, size=(h, w, 3), dtype=np.uint16).astype(">u2")
+        full = r2p.Image.make(w, h, 3, 2, r2p.WINDOW_NONE)
+    want, win = expected_filtered(O, r2p, full, raw)
+    rb = full.row_bytes
+    raw8 = np.ascontiguousarray(raw).view(np.uint8).reshape(h, -1)
+    last = r2p.DeviceBuffer(rb)
+    prior = None
+    parts = []
+    for r0 in range(0, h, strip):
+        n = min(strip, h - r0)
+        img = r2p.Image.make(w, n, full.channels, full.bytes_per_sample, full.window_mode, full.dicom)
+        d_raw = r2p.DeviceBuffer.from_array(np.ascontiguousarray(raw8[r0:r0 + n]))
+        d_out = r2p.DeviceBuffer(img.filtered_bytes + 16)
+        new_last = r2p.DeviceBuffer(rb)
+        engine.window_filter_device(img, d_raw.ptr, d_out.ptr, d_prior=prior, d_last_row=new_last.ptr)
+        parts.append(d_out.download(img.filtered_bytes))
+        got_last = new_last.download(rb)
+        assert np.array_equal(got_last, win.reshape(h, rb)[r0 + n - 1]), "carried row differs from the oracle"
+        last = new_last
+        prior = last.ptr
+    assert np.array_equal(np.concatenate(parts), want)
