@@ -64,8 +64,11 @@ __device__ __forceinline__ uint32_t ld32u(const uint8_t* base, int p)
     return fshr(w[q], w[q + 1], (uint32_t)(p & 3) << 3);
 }
 
-template <int HB>
-__device__ __forceinline__ uint32_t hash4(uint32_t v) { return (v * 2654435761u) >> (32 - HB); }
+// Multiplicative hash of 4 bytes to hb bits.
+__device__ __forceinline__ uint32_t hash4(uint32_t v, int hb) { return (v * 2654435761u) >> (32 - hb); }
+
+// An image's hash table bits: 10 or 11.
+__device__ __forceinline__ int lz_hash_bits(const DevImage& d) { return d.hash_bits == 10 ? 10 : 11; }
 
 // Fixed-Huffman code of a literal byte: reversed code and its length.
 __device__ __forceinline__ void lit_code(uint32_t b, uint32_t& v, int& n)
@@ -111,8 +114,7 @@ __device__ __forceinline__ void match_code(int len, int dist, uint32_t& v, int& 
 // Greedy parse of in[s, e) by one thread into the word buffer `ob`.
 // `tab` is the warp's shared hash table (latest position + 1 per hash).
 // Returns the number of bits written; the last partial word is stored too.
-template <int HB>
-__device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, uint16_t* tab, uint32_t* ob)
+__device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb, uint16_t* tab, uint32_t* ob)
 {
     const bool vert = rb1 > 1 && rb1 <= kMaxDist;
     uint64_t acc = 0;
@@ -123,7 +125,7 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, uint16_
         int L = 0, D = 0;
         if (p + 4 <= e) {
             const uint32_t w = ld32u(in, p);
-            const uint32_t h = hash4<HB>(w);
+            const uint32_t h = hash4(w, hb);
             const int t = tab[h];
             tab[h] = (uint16_t)(p + 1);
             if (p > 0 && w == (uint32_t)in[p - 1] * 0x01010101u) {
@@ -192,7 +194,6 @@ __device__ void cta_adler_sums(const uint8_t* buf, int n, uint32_t& s1_out, uint
     s2_out = cta_sum64<NT>(s2, red64);
 }
 
-template <int HB>
 __global__ void __launch_bounds__(kLzThreads, 1)
 k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int max_block,
               uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
@@ -209,9 +210,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     __shared__ uint32_t wsum[kLzWarps];
     __shared__ uint32_t s_info[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int kHashSize = 1 << HB;
     build_crc_tables(ctab);
-    uint16_t* mytab = tabs + warp * kHashSize;
     uint32_t* myout = outs + tid * lw;
 
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
@@ -221,6 +220,8 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         const int n = (int)bo.in_len;
         const uint8_t* src = d.filt + bo.in_off;
         const bool last = ((int)(b - d.blk0) == d.nblocks - 1) && !d.open_end;
+        const int hb = lz_hash_bits(d);
+        uint16_t* mytab = tabs + (warp << hb);      // the launch sized the tables for the largest hb
         __syncthreads();
         // stage the block (+ zero padding), clear the hash tables
         if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
@@ -231,7 +232,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             for (int i = tid; i < n; i += kLzThreads) in[i] = src[i];
         }
         for (int i = n + tid; i < in_bytes; i += kLzThreads) in[i] = 0;
-        for (int i = tid; i < kLzWarps * kHashSize / 2; i += kLzThreads) reinterpret_cast<uint32_t*>(tabs)[i] = 0u;
+        for (int i = tid; i < (kLzWarps << hb) / 2; i += kLzThreads) reinterpret_cast<uint32_t*>(tabs)[i] = 0u;
         __syncthreads();
         uint32_t s1;
         uint64_t s2;
@@ -241,12 +242,12 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         const int ws0 = min(n, warp * 32 * sub);
         for (int q0 = max(0, ws0 - kPrefill); q0 < ws0; q0 += 32) {
             const int q = q0 + lane;
-            if (q < ws0 && q + 4 <= n) mytab[hash4<HB>(ld32u(in, q))] = (uint16_t)(q + 1);
+            if (q < ws0 && q + 4 <= n) mytab[hash4(ld32u(in, q), hb)] = (uint16_t)(q + 1);
             __syncwarp();
         }
         // parse this thread's sub-range
         const int s = min(n, tid * sub), e = min(n, s + sub);
-        const uint32_t nbits = (s < e) ? parse_lane<HB>(in, s, e, d.rb + 1, mytab, myout) : 0u;
+        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, d.rb + 1, hb, mytab, myout) : 0u;
         // CTA-wide exclusive scan of the bit counts
         uint32_t incl = nbits;
 #pragma unroll
@@ -320,24 +321,16 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     }
 }
 
-template <int HB>
-static cudaError_t launch_lz77_hb(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
-                                  uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s)
-{
-    const int smem = lz_smem_bytes(max_block, HB);
-    cudaError_t e = cudaFuncSetAttribute(k_lz77_blocks<HB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    k_lz77_blocks<HB><<<grid, kLzThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
-    note_launch();
-    return cudaGetLastError();
-}
-
+// hash_bits: the largest table size among the launch's images (10 or 11).
 cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
                         uint64_t slot_bytes, const uint32_t* xpow, int grid, int hash_bits, cudaStream_t s)
 {
-    if (hash_bits == 10)
-        return launch_lz77_hb<10>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow, grid, s);
-    return launch_lz77_hb<11>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow, grid, s);
+    const int smem = lz_smem_bytes(max_block, hash_bits == 10 ? 10 : 11);
+    cudaError_t e = cudaFuncSetAttribute(k_lz77_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_lz77_blocks<<<grid, kLzThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    note_launch();
+    return cudaGetLastError();
 }
 
 }  // namespace r2p

@@ -302,7 +302,7 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
     const int cps = P.smem > 0 ? filter_ctas_per_sm(P.smem) : 1;
     P.slots_total = e->nsm * cps;
     uint64_t lut_total = 0, filt_total = 0;
-    int hb_votes[2] = {0, 0};
+    bool any11 = false;
     for (int i = 0; i < n; i++) {
         DevImage& d = plans[i].di;
         if (P.smem > 0) {
@@ -332,12 +332,13 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
         P.nblk += (uint32_t)d.nblocks;
         P.max_block = std::max(P.max_block, d.block_size);
         if (d.level == 0) P.any_stored = true; else P.any_lz = true;
-        if (d.level > 0) hb_votes[plans[i].hash_bits == 10 ? 0 : 1] += d.nblocks;
+        d.hash_bits = plans[i].hash_bits == 10 ? 10 : 11;
+        if (d.level > 0 && d.hash_bits == 11) any11 = true;
         lut_total += plans[i].lut_cap;
         if (!cb.filt[i]) filt_total += align_up(d.filt_bytes + 64, 256);
     }
     // one hash-table size per launch: the one most blocks were tuned for
-    P.hash_bits = hb_votes[0] > hb_votes[1] ? 10 : 11;
+    P.hash_bits = any11 ? 11 : 10;     // LZ77 tables sized for the largest; each block uses its image's
     P.slot = P.any_lz ? lz77_slot_bytes(P.max_block) : 0;
     Layout L;
     P.o_img = L.take(sizeof(DevImage) * n);

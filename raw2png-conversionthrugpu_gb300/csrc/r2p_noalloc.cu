@@ -75,6 +75,7 @@ __global__ void k_noalloc_plan(DevImage* d, BlockOut* bo, const uint8_t* in, uin
         z.filt = const_cast<uint8_t*>(in);
         z.level = level;
         z.block_size = bs;
+        z.hash_bits = 11;
         z.nblocks = nb;
         z.out_kind = 1;
         z.prefix = 2;
