@@ -279,114 +279,144 @@ struct WinCtx {
     r2p_dicom_params dp;
 };
 
-__device__ __forceinline__ uint32_t lut_get(const WinCtx& w, uint32_t idx)
+// Windowing kinds: the resolved WinMode split by sample and table sizes, so
+// each row loop is compiled for exactly one transform.
+enum WinKind : int {
+    K_COPY = 0,      // bytes unchanged
+    K_SWAP16 = 1,    // 16-bit LE -> BE
+    K_LUT16 = 2,     // 16-bit in/out through a u16 table (entries in PNG byte order)
+    K_LUT8IN = 3,    // 8-bit in/out through a u8 table
+    K_DIRECT = 4,    // DICOM formula per sample (table too large)
+    K_Q15 = 5,       // 16-bit in, 8-bit out, Q15 linear map
+    K_LUT8 = 6,      // 16-bit in, 8-bit out, FP32-built table
+};
+
+__device__ __forceinline__ int win_kind(const WinCtx& w)
 {
-    if (w.ob == 2) return reinterpret_cast<const uint16_t*>(w.lut)[idx];
-    return w.lut[idx];
+    switch (w.mode) {
+        case W_COPY: return K_COPY;
+        case W_SWAP16: return K_SWAP16;
+        case W_A2_LUT: return w.ib == 2 ? K_LUT16 : K_LUT8IN;
+        case W_Q15: return K_Q15;
+        case W_LUT8: return K_LUT8;
+        default: return K_DIRECT;
+    }
 }
 
-// Window one 16-bit LE sample to an 8-bit output value (Q15 / LUT8 modes).
-__device__ __forceinline__ uint32_t win8(const WinCtx& w, uint32_t raw)
+// DICOM formula on one sample, in PNG byte order (kept out of line: rare).
+__device__ __noinline__ uint32_t win_direct(const WinCtx& w, uint32_t raw)
 {
-    if (w.mode == W_Q15) {
+    const uint32_t m = (w.ib == 2) ? win_index(raw, w.shift, w.mask) : raw;
+    const uint32_t v = a2_eval(m, w.dp);
+    return (w.ob == 2) ? (((v & 0xFF) << 8) | (v >> 8)) : v;
+}
+
+// One sample (16-bit LE value or byte) of kind K; output in the low ob bytes,
+// PNG byte order.
+template <int K>
+__device__ __forceinline__ uint32_t win_sample(const WinCtx& w, uint32_t raw)
+{
+    if (K == K_COPY) return raw;
+    if (K == K_SWAP16) return ((raw & 0xFF) << 8) | (raw >> 8);
+    if (K == K_LUT16) return reinterpret_cast<const uint16_t*>(w.lut)[win_index(raw, w.shift, w.mask)];
+    if (K == K_LUT8IN) return w.lut[raw & w.mask];
+    if (K == K_Q15) {
         const int32_t x = (w.dp.pixel_rep == 1) ? (int32_t)(int16_t)(uint16_t)raw : (int32_t)raw;
         const int32_t v = (int32_t)((uint32_t)x * (uint32_t)w.qa + (uint32_t)w.qb) >> 15;
         return (uint32_t)(v < 0 ? 0 : v > 255 ? 255 : v);
     }
-    return w.lut[(raw >> w.shift) & w.mask];
+    if (K == K_LUT8) return w.lut[(raw >> w.shift) & w.mask];
+    return win_direct(w, raw);
 }
 
-// Window one sample with output depth = input depth; result in PNG byte order
-// packed in the low ob bytes (16-bit: byte 0 = MSB).
-__device__ __forceinline__ uint32_t winN(const WinCtx& w, uint32_t raw)
+// 16 raw bytes (one aligned unit) -> windowed output: 16 bytes (same depth)
+// or 8 bytes (16 -> 8 bit, in o[0..1]).
+template <int K>
+__device__ __forceinline__ void win_unit(const WinCtx& w, const uint4 v, uint32_t o[4])
 {
-    switch (w.mode) {
-        case W_COPY: return raw;                                   // raw already in memory order
-        case W_SWAP16: return ((raw & 0xFF) << 8) | (raw >> 8);
-        case W_A2_LUT: return lut_get(w, win_index(raw, w.shift, w.mask));
-        default: {                                                 // W_A2_DIRECT
-            uint32_t m = raw;
-            if (w.ib == 2) m = win_index(raw, w.shift, w.mask);
-            const uint32_t v = a2_eval(m, w.dp);
-            return (w.ob == 2) ? (((v & 0xFF) << 8) | (v >> 8)) : v;
+    const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+    if (K == K_COPY) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) o[k] = wv[k];
+    } else if (K == K_SWAP16) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) o[k] = __byte_perm(wv[k], 0, 0x2301);
+    } else if (K == K_Q15 || K == K_LUT8) {
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+            o[k] = win_sample<K>(w, wv[2 * k] & 0xFFFF) | (win_sample<K>(w, wv[2 * k] >> 16) << 8) |
+                   (win_sample<K>(w, wv[2 * k + 1] & 0xFFFF) << 16) | (win_sample<K>(w, wv[2 * k + 1] >> 16) << 24);
+        o[2] = o[3] = 0;
+    } else if (K == K_LUT16 || K == K_DIRECT) {
+        if (K == K_LUT16 || w.ib == 2) {                         // 16-bit samples
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                o[k] = win_sample<K>(w, wv[k] & 0xFFFF) | (win_sample<K>(w, wv[k] >> 16) << 16);
+            return;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {                              // K_DIRECT on 8-bit samples
+            uint32_t acc = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc |= win_sample<K>(w, (wv[k] >> (8 * q)) & 0xFF) << (8 * q);
+            o[k] = acc;
+        }
+    } else {                                                       // K_LUT8IN: 8-bit samples
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t acc = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc |= win_sample<K>(w, (wv[k] >> (8 * q)) & 0xFF) << (8 * q);
+            o[k] = acc;
         }
     }
 }
 
-// Window raw row `r` of image d into smem row `dst` (rb bytes) and zero its tail.
-__device__ void window_row_range(const DevImage& d, const WinCtx& w, int r, uint8_t* dst, int tid,
-                                 int nthr, bool aligned)
+// Window raw row `r` of image d into smem row `dst` (rb bytes) with plain
+// global loads and zero its tail.  aligned: rows are 16-byte multiples at a
+// 16-byte aligned base (whole units); otherwise one 4-byte output group per
+// thread from byte loads.
+template <int K>
+__device__ void window_row_k(const DevImage& d, const WinCtx& w, int r, uint8_t* dst, int tid, int nthr, bool aligned)
 {
     const uint8_t* src = d.raw + (size_t)r * (size_t)d.in_pitch;
+    constexpr bool to8 = (K == K_Q15 || K == K_LUT8);
     if (aligned) {
         const int units = d.in_pitch >> 4;
         const uint4* s4 = reinterpret_cast<const uint4*>(src);
         for (int u = tid; u < units; u += nthr) {
-            const uint4 v = __ldg(s4 + u);
-            const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-            if (w.ob == w.ib) {
-                uint32_t o[4];
-                if (w.mode == W_COPY) {
-                    o[0] = wv[0]; o[1] = wv[1]; o[2] = wv[2]; o[3] = wv[3];
-                } else if (w.ib == 2) {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        const uint32_t lo = winN(w, wv[k] & 0xFFFF);
-                        const uint32_t hi = winN(w, wv[k] >> 16);
-                        o[k] = lo | (hi << 16);
-                    }
-                } else {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        uint32_t acc = 0;
-#pragma unroll
-                        for (int j = 0; j < 4; j++) acc |= winN(w, (wv[k] >> (8 * j)) & 0xFF) << (8 * j);
-                        o[k] = acc;
-                    }
-                }
-                *reinterpret_cast<uint4*>(dst + 16 * u) = make_uint4(o[0], o[1], o[2], o[3]);
-            } else {
-                uint32_t o[2];
-#pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const uint32_t s0 = win8(w, wv[2 * k] & 0xFFFF), s1 = win8(w, wv[2 * k] >> 16);
-                    const uint32_t s2 = win8(w, wv[2 * k + 1] & 0xFFFF), s3 = win8(w, wv[2 * k + 1] >> 16);
-                    o[k] = s0 | (s1 << 8) | (s2 << 16) | (s3 << 24);
-                }
-                *reinterpret_cast<uint2*>(dst + 8 * u) = make_uint2(o[0], o[1]);
-            }
+            uint32_t o[4];
+            win_unit<K>(w, __ldg(s4 + u), o);
+            if (to8) *reinterpret_cast<uint2*>(dst + 8 * u) = make_uint2(o[0], o[1]);
+            else     *reinterpret_cast<uint4*>(dst + 16 * u) = make_uint4(o[0], o[1], o[2], o[3]);
         }
     } else {
-        // Any alignment: one output byte group of 4 per thread, byte loads.
         const int groups = (d.rb + 3) >> 2;
         for (int g = tid; g < groups; g += nthr) {
             uint32_t o = 0;
             const int b0 = 4 * g;
-            if (w.ob == w.ib) {
-                if (w.ib == 2) {
+            if (to8) {
 #pragma unroll
-                    for (int j = 0; j < 2; j++) {
-                        const int bo = b0 + 2 * j;
-                        if (bo < d.rb) {
-                            const uint32_t raw = (uint32_t)__ldg(src + bo) | ((uint32_t)__ldg(src + bo + 1) << 8);
-                            o |= winN(w, raw) << (16 * j);
-                        }
-                    }
-                } else {
+                for (int j = 0; j < 4; j++) {
+                    const int so = 2 * (b0 + j);
+                    if (b0 + j < d.rb)
+                        o |= win_sample<K>(w, (uint32_t)__ldg(src + so) | ((uint32_t)__ldg(src + so + 1) << 8)) << (8 * j);
+                }
+            } else if (d.ib == 2) {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const int bo = b0 + j;
-                        if (bo < d.rb) o |= winN(w, __ldg(src + bo)) << (8 * j);
+                for (int j = 0; j < 2; j++) {
+                    const int bo = b0 + 2 * j;
+                    if (bo < d.rb) {
+                        const uint32_t raw = (uint32_t)__ldg(src + bo) | ((uint32_t)__ldg(src + bo + 1) << 8);
+                        // K_COPY keeps memory order: the little-endian pair is the bytes as they lie
+                        o |= win_sample<K>(w, raw) << (16 * j);
                     }
                 }
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const int so = 2 * (b0 + j);
-                    if (b0 + j < d.rb) {
-                        const uint32_t raw = (uint32_t)__ldg(src + so) | ((uint32_t)__ldg(src + so + 1) << 8);
-                        o |= win8(w, raw) << (8 * j);
-                    }
+                    const int bo = b0 + j;
+                    if (bo < d.rb) o |= win_sample<K>(w, __ldg(src + bo)) << (8 * j);
                 }
             }
             if (b0 + 4 <= d.rb) {
@@ -401,17 +431,18 @@ __device__ void window_row_range(const DevImage& d, const WinCtx& w, int r, uint
     for (int i = tail0 + tid; i < tail1; i += nthr) dst[i] = 0;
 }
 
-// Row words: X = current row, U = row above; word k covers bytes 4k..4k+3.
-__device__ __forceinline__ void load_xabc(const uint32_t* X, const uint32_t* U, int k, int bpp,
-                                          uint32_t& x, uint32_t& a, uint32_t& b, uint32_t& c)
+__device__ void window_row_range(const DevImage& d, const WinCtx& w, int r, uint8_t* dst, int tid, int nthr,
+                                 bool aligned)
 {
-    const int off = 4 * k - bpp;
-    const int w0 = off >> 2;                 // floor division (guard words cover w0 >= -2)
-    const uint32_t sh = (uint32_t)(off & 3) << 3;
-    x = X[k];
-    b = U[k];
-    a = fshr(X[w0], X[w0 + 1], sh);
-    c = fshr(U[w0], U[w0 + 1], sh);
+    switch (win_kind(w)) {
+        case K_COPY: window_row_k<K_COPY>(d, w, r, dst, tid, nthr, aligned); break;
+        case K_SWAP16: window_row_k<K_SWAP16>(d, w, r, dst, tid, nthr, aligned); break;
+        case K_LUT16: window_row_k<K_LUT16>(d, w, r, dst, tid, nthr, aligned); break;
+        case K_LUT8IN: window_row_k<K_LUT8IN>(d, w, r, dst, tid, nthr, aligned); break;
+        case K_Q15: window_row_k<K_Q15>(d, w, r, dst, tid, nthr, aligned); break;
+        case K_LUT8: window_row_k<K_LUT8>(d, w, r, dst, tid, nthr, aligned); break;
+        default: window_row_k<K_DIRECT>(d, w, r, dst, tid, nthr, aligned); break;
+    }
 }
 
 __device__ __forceinline__ uint8_t filtered_byte(const uint8_t* xr, const uint8_t* ur, int i, int bpp, int f)
@@ -421,50 +452,191 @@ __device__ __forceinline__ uint8_t filtered_byte(const uint8_t* xr, const uint8_
     return (uint8_t)filter_word(f, x, a, b, c);
 }
 
+
 // Window n staged raw rows (16-byte multiples, in shared memory) into their
-// ring slots.  All threads; no division: rows outer, 16-byte units inner.
-__device__ void window_staged_rows(const DevImage& d, const WinCtx& w, const uint8_t* stage, int n,
-                                   uint8_t* ring, int stride, int slots, int rel0, int tid, int nthr)
+// ring slots.  All threads; rows outer, 16-byte units inner.
+template <int K>
+__device__ void window_staged_k(const DevImage& d, const WinCtx& w, const uint8_t* stage, int n, uint8_t* ring,
+                                int stride, int slots, int rel0, int tid, int nthr)
 {
+    constexpr bool to8 = (K == K_Q15 || K == K_LUT8);
     const int units = d.in_pitch >> 4;
+    const int tail0 = d.rb, tail1 = ((d.rb + 15) & ~15) + 16;
     for (int j = 0; j < n; j++) {
         const uint4* s4 = reinterpret_cast<const uint4*>(stage + (size_t)j * d.in_pitch);
         uint8_t* dst = ring + ((rel0 + j) % slots) * stride + 16;
-        if (w.mode == W_COPY) {
-            for (int u = tid; u < units; u += nthr) reinterpret_cast<uint4*>(dst)[u] = s4[u];
-        } else if (w.ob == w.ib) {
-            for (int u = tid; u < units; u += nthr) {
-                const uint4 v = s4[u];
-                const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-                uint32_t o[4];
-                if (w.ib == 2) {
-#pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        o[k] = winN(w, wv[k] & 0xFFFF) | (winN(w, wv[k] >> 16) << 16);
-                } else {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        uint32_t acc = 0;
-#pragma unroll
-                        for (int q = 0; q < 4; q++) acc |= winN(w, (wv[k] >> (8 * q)) & 0xFF) << (8 * q);
-                        o[k] = acc;
-                    }
-                }
-                reinterpret_cast<uint4*>(dst)[u] = make_uint4(o[0], o[1], o[2], o[3]);
-            }
-        } else {
-            for (int u = tid; u < units; u += nthr) {
-                const uint4 v = s4[u];
-                const uint32_t o0 = win8(w, v.x & 0xFFFF) | (win8(w, v.x >> 16) << 8) |
-                                    (win8(w, v.y & 0xFFFF) << 16) | (win8(w, v.y >> 16) << 24);
-                const uint32_t o1 = win8(w, v.z & 0xFFFF) | (win8(w, v.z >> 16) << 8) |
-                                    (win8(w, v.w & 0xFFFF) << 16) | (win8(w, v.w >> 16) << 24);
-                reinterpret_cast<uint2*>(dst)[u] = make_uint2(o0, o1);
-            }
+        for (int u = tid; u < units; u += nthr) {
+            uint32_t o[4];
+            win_unit<K>(w, s4[u], o);
+            if (to8) reinterpret_cast<uint2*>(dst)[u] = make_uint2(o[0], o[1]);
+            else     reinterpret_cast<uint4*>(dst)[u] = make_uint4(o[0], o[1], o[2], o[3]);
         }
-        const int tail0 = d.rb, tail1 = ((d.rb + 15) & ~15) + 16;
         for (int i = tail0 + tid; i < tail1; i += nthr) dst[i] = 0;
     }
+}
+
+__device__ void window_staged_rows(const DevImage& d, const WinCtx& w, const uint8_t* stage, int n, uint8_t* ring,
+                                   int stride, int slots, int rel0, int tid, int nthr)
+{
+    switch (win_kind(w)) {
+        case K_COPY: window_staged_k<K_COPY>(d, w, stage, n, ring, stride, slots, rel0, tid, nthr); break;
+        case K_SWAP16: window_staged_k<K_SWAP16>(d, w, stage, n, ring, stride, slots, rel0, tid, nthr); break;
+        case K_LUT16: window_staged_k<K_LUT16>(d, w, stage, n, ring, stride, slots, rel0, tid, nthr); break;
+        case K_LUT8IN: window_staged_k<K_LUT8IN>(d, w, stage, n, ring, stride, slots, rel0, tid, nthr); break;
+        case K_Q15: window_staged_k<K_Q15>(d, w, stage, n, ring, stride, slots, rel0, tid, nthr); break;
+        case K_LUT8: window_staged_k<K_LUT8>(d, w, stage, n, ring, stride, slots, rel0, tid, nthr); break;
+        default: window_staged_k<K_DIRECT>(d, w, stage, n, ring, stride, slots, rel0, tid, nthr); break;
+    }
+}
+
+// One 16-byte unit of a windowed row (u >= 0) and the two words before it
+// (the slot's 16 guard bytes are zero, so unit 0 sees zeros on its left).
+struct RowUnit {
+    uint32_t m2, m1, w[4];
+};
+
+__device__ __forceinline__ RowUnit load_unit(const uint8_t* row, int u)
+{
+    const uint4 v = *reinterpret_cast<const uint4*>(row + 16 * u);
+    const uint2 p = *reinterpret_cast<const uint2*>(row + 16 * u - 8);
+    RowUnit r;
+    r.m2 = p.x; r.m1 = p.y;
+    r.w[0] = v.x; r.w[1] = v.y; r.w[2] = v.z; r.w[3] = v.w;
+    return r;
+}
+
+// Words of the bytes bpp to the left of the unit's four words.  DW = words
+// reached back (1 for bpp <= 4, 2 for bpp 6 or 8); sh = 8 * (4 * DW - bpp).
+template <int DW>
+__device__ __forceinline__ void left_words(const RowUnit& r, uint32_t sh, uint32_t out[4])
+{
+    if (DW == 1) {
+        out[0] = fshr(r.m1, r.w[0], sh);
+        out[1] = fshr(r.w[0], r.w[1], sh);
+        out[2] = fshr(r.w[1], r.w[2], sh);
+        out[3] = fshr(r.w[2], r.w[3], sh);
+    } else {
+        out[0] = fshr(r.m2, r.m1, sh);
+        out[1] = fshr(r.m1, r.w[0], sh);
+        out[2] = fshr(r.w[0], r.w[1], sh);
+        out[3] = fshr(r.w[1], r.w[2], sh);
+    }
+}
+
+// Byte mask of word q of a unit with nvalid valid bytes.
+__device__ __forceinline__ uint32_t unit_word_mask(int nvalid, int q)
+{
+    const int k = nvalid - 4 * q;
+    return k >= 4 ? 0xFFFFFFFFu : k <= 0 ? 0u : ((1u << (8 * k)) - 1u);
+}
+
+// Scores of units [us, ue) of one row, this warp's share.
+template <int DW>
+__device__ __forceinline__ Score5 score_units(const uint8_t* xr, const uint8_t* ur, int us, int ue, int rb, uint32_t sh,
+                                              int lane)
+{
+    Score5 s = {0u, 0u, 0u, 0u, 0u};
+    for (int u = us + lane; u < ue; u += 32) {
+        const RowUnit X = load_unit(xr, u), B = load_unit(ur, u);
+        uint32_t a[4], c[4];
+        left_words<DW>(X, sh, a);
+        left_words<DW>(B, sh, c);
+        const int nvalid = rb - 16 * u;
+        if (nvalid >= 16) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) score_word(s, X.w[q], a[q], B.w[q], c[q], 0xFFFFFFFFu);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) score_word(s, X.w[q], a[q], B.w[q], c[q], unit_word_mask(nvalid, q));
+        }
+    }
+    return s;
+}
+
+// Filtered word of filter type F (compile-time).
+template <int F>
+__device__ __forceinline__ uint32_t filter_word_t(uint32_t x, uint32_t a, uint32_t b, uint32_t c)
+{
+    if (F == 0) return x;
+    if (F == 1) return sub4(x, a);
+    if (F == 2) return sub4(x, b);
+    if (F == 3) return sub4(x, avg4(a, b));
+    return sub4(x, R2P_PAETH4(a, b, c));
+}
+
+// Filtered words (type F) of units [us, ue), stored as 4-byte words aligned to
+// the output: gw = the aligned word holding data byte 0 minus e bytes, words
+// klo..khi lie wholly inside the row; the rest is written byte-wise by the caller.
+template <int DW, int F>
+__device__ __forceinline__ void store_units_t(const uint8_t* xr, const uint8_t* ur, int us, int ue, uint32_t sh,
+                                              uint32_t* gw, int e, int klo, int khi, int lane)
+{
+    uint32_t carry = 0;                       // last filtered word of the unit before this lane's
+    if (us > 0) {
+        const RowUnit X = load_unit(xr, us - 1), B = load_unit(ur, us - 1);
+        uint32_t a[4], c[4];
+        left_words<DW>(X, sh, a);
+        left_words<DW>(B, sh, c);
+        carry = filter_word_t<F>(X.w[3], a[3], B.w[3], c[3]);
+    }
+    const uint32_t es = 8u * (uint32_t)e;
+    for (int u0 = us; u0 < ue; u0 += 32) {
+        const int u = u0 + lane;
+        uint32_t Fw[4] = {0u, 0u, 0u, 0u};
+        if (u < ue) {
+            const RowUnit X = load_unit(xr, u), B = load_unit(ur, u);
+            uint32_t a[4], c[4];
+            left_words<DW>(X, sh, a);
+            left_words<DW>(B, sh, c);
+#pragma unroll
+            for (int q = 0; q < 4; q++) Fw[q] = filter_word_t<F>(X.w[q], a[q], B.w[q], c[q]);
+        }
+        uint32_t Fp = __shfl_up_sync(0xFFFFFFFFu, Fw[3], 1);
+        const uint32_t last = __shfl_sync(0xFFFFFFFFu, Fw[3], 31);
+        if (lane == 0) Fp = carry;
+        carry = last;
+        if (u < ue) {
+            const int k0 = 4 * u;
+            if (k0 >= klo && k0 + 3 <= khi) {             // the whole unit is interior
+                if (e) {
+                    gw[k0] = __funnelshift_l(Fp, Fw[0], es);
+                    gw[k0 + 1] = __funnelshift_l(Fw[0], Fw[1], es);
+                    gw[k0 + 2] = __funnelshift_l(Fw[1], Fw[2], es);
+                    gw[k0 + 3] = __funnelshift_l(Fw[2], Fw[3], es);
+                } else {
+                    gw[k0] = Fw[0]; gw[k0 + 1] = Fw[1]; gw[k0 + 2] = Fw[2]; gw[k0 + 3] = Fw[3];
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int k = k0 + q;
+                    const uint32_t prevw = q == 0 ? Fp : Fw[q - 1];
+                    if (k >= klo && k <= khi) gw[k] = e ? __funnelshift_l(prevw, Fw[q], es) : Fw[q];
+                }
+            }
+        }
+    }
+}
+
+template <int DW>
+__device__ __forceinline__ void store_units(const uint8_t* xr, const uint8_t* ur, int us, int ue, uint32_t sh, int f,
+                                            uint32_t* gw, int e, int klo, int khi, int lane)
+{
+    switch (f) {
+        case 0: store_units_t<DW, 0>(xr, ur, us, ue, sh, gw, e, klo, khi, lane); break;
+        case 1: store_units_t<DW, 1>(xr, ur, us, ue, sh, gw, e, klo, khi, lane); break;
+        case 2: store_units_t<DW, 2>(xr, ur, us, ue, sh, gw, e, klo, khi, lane); break;
+        case 3: store_units_t<DW, 3>(xr, ur, us, ue, sh, gw, e, klo, khi, lane); break;
+        default: store_units_t<DW, 4>(xr, ur, us, ue, sh, gw, e, klo, khi, lane); break;
+    }
+}
+
+// Barrier over the nthreads threads (a multiple of 32) of one row group; ids
+// 1..15 (0 is __syncthreads).  Every warp of the group executes the same
+// sequence of these.
+__device__ __forceinline__ void group_sync(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
 // Time limit for one bulk copy of a tile to land in shared memory.
@@ -567,28 +739,21 @@ k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items,
                 __syncthreads();
             }
 
-            const int nwords = (rb + 3) >> 2;
+            const int nunits = (rb + 15) >> 4;
             const int g = warp / G, wg = warp % G;
-            int seg = (nwords + G - 1) / G;
-            seg = (seg + 31) & ~31;
-            const int ws = wg * seg, we = min(nwords, ws + seg);
+            const int useg = (nunits + G - 1) / G;
+            const int us = min(nunits, wg * useg), ue = min(nunits, us + useg);
+            const int dw = (bpp + 3) >> 2;                   // words reached back: 1 or 2
+            const uint32_t sh = 8u * (uint32_t)(4 * dw - bpp);
             for (int pass = 0; pass * rpp < n; pass++) {
                 const int j = pass * rpp + g;                // tile row index of this group
                 const bool active = j < n;
                 const int rel = rel0 + j;
                 const uint8_t* xr = ring + (rel % slots) * stride + 16;
                 const uint8_t* ur = ring + ((rel - 1 + slots) % slots) * stride + 16;
-                const uint32_t* X = reinterpret_cast<const uint32_t*>(xr);
-                const uint32_t* U = reinterpret_cast<const uint32_t*>(ur);
                 Score5 s = {0u, 0u, 0u, 0u, 0u};
-                if (active) {
-                    const uint32_t tailmask = (rb & 3) ? ((1u << (8 * (rb & 3))) - 1u) : 0xFFFFFFFFu;
-                    for (int k = ws + lane; k < we; k += 32) {
-                        uint32_t x, a, b, c;
-                        load_xabc(X, U, k, bpp, x, a, b, c);
-                        score_word(s, x, a, b, c, (k == nwords - 1) ? tailmask : 0xFFFFFFFFu);
-                    }
-                }
+                if (active)
+                    s = dw == 1 ? score_units<1>(xr, ur, us, ue, rb, sh, lane) : score_units<2>(xr, ur, us, ue, rb, sh, lane);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     s.s0 += __shfl_xor_sync(0xFFFFFFFFu, s.s0, o);
@@ -597,19 +762,19 @@ k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items,
                     s.s3 += __shfl_xor_sync(0xFFFFFFFFu, s.s3, o);
                     s.s4 += __shfl_xor_sync(0xFFFFFFFFu, s.s4, o);
                 }
-                if (G > 1) {
+                if (G > 1) {                                 // combine the group's warps
                     if (lane == 0) {
                         red[warp][0] = s.s0; red[warp][1] = s.s1; red[warp][2] = s.s2;
                         red[warp][3] = s.s3; red[warp][4] = s.s4;
                     }
-                    __syncthreads();
+                    group_sync(1 + g, 32 * G);
                     Score5 t = {0u, 0u, 0u, 0u, 0u};
                     for (int q = g * G; q < g * G + G; q++) {
                         t.s0 += red[q][0]; t.s1 += red[q][1]; t.s2 += red[q][2];
                         t.s3 += red[q][3]; t.s4 += red[q][4];
                     }
                     s = t;
-                    __syncthreads();
+                    group_sync(1 + g, 32 * G);                   // red[] is reused by the next pass
                 }
                 if (!active) continue;
                 const int f = best_filter(s);
@@ -624,28 +789,8 @@ k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items,
                 // interior words: k in [klo, khi]
                 const int klo = (e > 0) ? 1 : 0;
                 const int khi = (e + rb - 4) >> 2;
-                uint32_t carry = 0;
-                if (ws > 0) {
-                    uint32_t x, a, b, c;
-                    load_xabc(X, U, ws - 1, bpp, x, a, b, c);
-                    carry = filter_word(f, x, a, b, c);
-                }
-                for (int k0 = ws; k0 < we; k0 += 32) {
-                    const int k = k0 + lane;
-                    uint32_t F = 0;
-                    if (k < we) {
-                        uint32_t x, a, b, c;
-                        load_xabc(X, U, k, bpp, x, a, b, c);
-                        F = filter_word(f, x, a, b, c);
-                    }
-                    uint32_t Fp = __shfl_up_sync(0xFFFFFFFFu, F, 1);
-                    const uint32_t last = __shfl_sync(0xFFFFFFFFu, F, 31);
-                    if (lane == 0) Fp = carry;
-                    carry = last;
-                    if (k < we && k >= klo && k <= khi) {
-                        gw[k] = e ? __funnelshift_l(Fp, F, 8u * (uint32_t)e) : F;
-                    }
-                }
+                if (dw == 1) store_units<1>(xr, ur, us, ue, sh, f, gw, e, klo, khi, lane);
+                else         store_units<2>(xr, ur, us, ue, sh, f, gw, e, klo, khi, lane);
                 // type byte, head bytes before the first interior word, tail bytes after the last
                 if (wg == 0 && lane == 0) {
                     orow[0] = (uint8_t)f;
@@ -677,13 +822,13 @@ int filter_lut_region(int mode, int lut_entries, int lut_esize)
     return lut_region_bytes(mode, lut_entries, lut_esize);
 }
 
-// Per-CTA shared memory aimed at two CTAs per SM; wider rows take more.
-constexpr int kFilterSmemTarget = 108 * 1024;
+// Per-CTA shared memory aimed at three CTAs per SM; wider rows take more.
+constexpr int kFilterSmemTarget = 72 * 1024;
 
 // Dynamic shared memory wanted for an image: LUT region, the staged raw rows
 // of one tile and tile+1 row slots, with the most rows (up to two passes of
-// the warp groups) that fit the two-CTA target, else the cap; -1 if even one
-// row does not fit.
+// the warp groups) that fit the three-CTA target, else the cap; -1 if even
+// one row does not fit.
 int filter_smem_bytes(int rb, int in_pitch, int mode, int lut_entries, int lut_esize)
 {
     const int lreg = lut_region_bytes(mode, lut_entries, lut_esize);

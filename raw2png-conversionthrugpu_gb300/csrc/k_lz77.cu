@@ -111,9 +111,20 @@ __device__ __forceinline__ void match_code(int len, int dist, uint32_t& v, int& 
     n = cl + lne + 5 + dne;
 }
 
+// 4 bytes at i >= -3 with bytes at negative indices read as zero.
+__device__ __forceinline__ uint32_t ld32z(const uint8_t* base, int i)
+{
+    if (i >= 0) return ld32u(base, i);
+    return i > -4 ? ld32u(base, 0) << (8 * -i) : 0u;
+}
+
 // Greedy parse of in[s, e) by one thread into the word buffer `ob`.
 // `tab` is the warp's shared hash table (latest position + 1 per hash).
 // Returns the number of bits written; the last partial word is stored too.
+//
+// The thread keeps three sliding registers -- w (bytes p..p+3), the byte
+// before p, and wv (bytes p-rb1..p-rb1+3, the scanline above) -- so a literal
+// step reads one new byte per stream instead of two words per candidate.
 __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb, uint16_t* tab, uint32_t* ob)
 {
     const bool vert = rb1 > 1 && rb1 <= kMaxDist;
@@ -121,16 +132,21 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb,
     int nacc = 0, nw = 0;
     uint32_t bits = 0;
     int p = s;
+    // sliding state for position p (bytes past the block end read the zero padding)
+    uint32_t w = ld32u(in, p);
+    // at the block start no run can match: a "previous byte" unequal to w's first byte
+    uint32_t prev = p > 0 ? (uint32_t)in[p - 1] : ((w & 0xFFu) ^ 1u);
+    // exact once p >= rb1 (the only positions it is compared at)
+    uint32_t wv = vert ? ld32z(in, max(p - rb1, -4)) : 0u;
     while (p < e) {
         int L = 0, D = 0;
         if (p + 4 <= e) {
-            const uint32_t w = ld32u(in, p);
             const uint32_t h = hash4(w, hb);
             const int t = tab[h];
             tab[h] = (uint16_t)(p + 1);
-            if (p > 0 && w == (uint32_t)in[p - 1] * 0x01010101u) {
+            if (w == prev * 0x01010101u) {
                 D = 1;
-            } else if (vert && p >= rb1 && ld32u(in, p - rb1) == w) {
+            } else if (vert && p >= rb1 && wv == w) {
                 D = rb1;
             } else if (t) {
                 const int dist = p - (t - 1);
@@ -155,8 +171,17 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb,
         if (L >= 4) {
             match_code(L, D, v, nb);
             p += L;
+            w = ld32u(in, p);
+            prev = in[p - 1];
+            wv = vert ? ld32z(in, max(p - rb1, -4)) : 0u;
         } else {
-            lit_code(in[p], v, nb);
+            lit_code(w & 0xFFu, v, nb);
+            prev = w & 0xFFu;
+            w = (w >> 8) | ((uint32_t)in[p + 4] << 24);
+            if (vert) {
+                const int q = p + 4 - rb1;
+                wv = (wv >> 8) | ((uint32_t)(q >= 0 ? in[q] : 0) << 24);
+            }
             p += 1;
         }
         acc |= (uint64_t)v << nacc;
@@ -194,7 +219,7 @@ __device__ void cta_adler_sums(const uint8_t* buf, int n, uint32_t& s1_out, uint
     s2_out = cta_sum64<NT>(s2, red64);
 }
 
-__global__ void __launch_bounds__(kLzThreads, 1)
+__global__ void __launch_bounds__(kLzThreads, 2)
 k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int max_block,
               uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
 {
@@ -240,7 +265,8 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         // seed the warp's table from the bytes before its range, oldest first
         const int sub = lz_sub_bytes(n);
         const int ws0 = min(n, warp * 32 * sub);
-        for (int q0 = max(0, ws0 - kPrefill); q0 < ws0; q0 += 32) {
+        const int prefill = min(kPrefill, d.block_size >> 4);          // ~one warp range of history
+        for (int q0 = max(0, ws0 - prefill); q0 < ws0; q0 += 32) {
             const int q = q0 + lane;
             if (q < ws0 && q + 4 <= n) mytab[hash4(ld32u(in, q), hb)] = (uint16_t)(q + 1);
             __syncwarp();

@@ -114,11 +114,17 @@ __device__ __forceinline__ uint32_t paeth4_dev(uint32_t a, uint32_t b, uint32_t 
 R2P_HD uint32_t cost4_acc(uint32_t v, uint32_t acc)
 {
     // sign = +1 or -1 per byte, then a signed byte dot product.
-    const uint32_t neg = (v >> 7) & kOnes;
-    const uint32_t sgn = neg * 0xFEu + kOnes;
 #if defined(__CUDA_ARCH__)
+    // PTX prmt (default mode): a selector nibble with its top bit set
+    // replicates the selected byte's sign bit, so 0xBA98 gives 0x00 or 0xFF
+    // per byte of v; OR 1 makes that +1 / -1 as signed bytes.
+    uint32_t neg;
+    asm("prmt.b32 %0, %1, 0, 0xBA98;" : "=r"(neg) : "r"(v));
+    const uint32_t sgn = neg | kOnes;
     return (uint32_t)__dp4a((int)v, (int)sgn, (int)acc);
 #else
+    const uint32_t neg = (v >> 7) & kOnes;
+    const uint32_t sgn = neg * 0xFEu + kOnes;
     int s = (int)acc;
     for (int k = 0; k < 4; k++)
         s += (int)(int8_t)(v >> (8 * k)) * (int)(int8_t)(sgn >> (8 * k));

@@ -312,9 +312,11 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
             if (plans[i].band_rows > 0) {
                 band_rows = ((uint64_t)plans[i].band_rows + T - 1) / T * T;    // tuned, whole tiles
             } else {
+                // about one band per resident CTA (a lone image), split evenly;
+                // a band's last tile may be partial
                 uint64_t nb = std::min<uint64_t>(ntiles, (uint64_t)P.slots_total);
                 if (n > 1) nb = std::min<uint64_t>(ntiles, std::max<uint64_t>(1, (uint64_t)P.slots_total / n + 1));
-                band_rows = ((ntiles + nb - 1) / nb) * T;
+                band_rows = (d.height + nb - 1) / nb;
             }
             for (uint64_t r = 0; r < d.height; r += band_rows)
                 P.items.push_back(BandItem{(uint32_t)i, (uint32_t)r,
