@@ -91,6 +91,22 @@ def build_ref(verbose=False):
     return True
 
 
+def build_ref_gpu_runner(verbose=False):
+    """oracle/_ref/libref_gpu_runner.so: a driver-API launcher for the
+    reference kernels in the cubins build_ref() made (on a machine with a
+    GPU driver; needs only the CUDA headers and the driver stub to build)."""
+    out = os.path.join(REF_DIR, "libref_gpu_runner.so")
+    src = os.path.join(HERE, "ref_gpu_runner.cpp")
+    if _newer(out, [src]):
+        return out
+    os.makedirs(REF_DIR, exist_ok=True)
+    cuda = os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"))
+    _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", src, "-I" + os.path.join(cuda, "include"),
+          "-L" + os.path.join(cuda, "lib64", "stubs"), "-L" + os.path.join(cuda, "lib64"), "-lcuda", "-o", out],
+         verbose)
+    return out
+
+
 if __name__ == "__main__":
     v = "-v" in sys.argv
     print(build_oracle(v))

@@ -1,0 +1,122 @@
+// ref_gpu_runner.cpp -- test infrastructure: launches the reference's own
+// window and filter kernels (dicom_preprocess_kernel, filter_select_kernel of
+// src/gpu_filter.cu, compiled from the reference sources into cubins by
+// oracle/build_oracle.py) through the CUDA driver API, with the launch shape
+// of the reference's host code (src/gpu_filter.cu:414-434: 256 threads, one
+// thread per sample for the window, one CTA per row for the filter).  Used
+// once, on a GPU, to record golden vectors (tests/golden/gen_gpu_golden.py);
+// nothing in the product loads it.
+#include <cuda.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+struct Mod {
+    CUmodule mod = nullptr;
+    CUfunction pre = nullptr, filt = nullptr;
+};
+
+std::vector<Mod> g_mods;
+CUcontext g_ctx = nullptr;
+std::string g_err;
+
+bool ck(CUresult r, const char* what)
+{
+    if (r == CUDA_SUCCESS) return true;
+    const char* s = nullptr;
+    cuGetErrorString(r, &s);
+    g_err = std::string(what) + ": " + (s ? s : "unknown error");
+    return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rgr_error(void) { return g_err.c_str(); }
+
+// Load a cubin; returns a handle >= 0 or -1.
+int rgr_open(const char* cubin)
+{
+    if (!g_ctx) {
+        CUdevice dev;
+        if (!ck(cuInit(0), "cuInit") || !ck(cuDeviceGet(&dev, 0), "cuDeviceGet") ||
+            !ck(cuDevicePrimaryCtxRetain(&g_ctx, dev), "cuDevicePrimaryCtxRetain"))
+            return -1;
+    }
+    if (!ck(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent")) return -1;
+    Mod m;
+    if (!ck(cuModuleLoad(&m.mod, cubin), "cuModuleLoad")) return -1;
+    unsigned int n = 0;
+    if (!ck(cuModuleGetFunctionCount(&n, m.mod), "cuModuleGetFunctionCount")) return -1;
+    std::vector<CUfunction> fs(n);
+    if (n && !ck(cuModuleEnumerateFunctions(fs.data(), n, m.mod), "cuModuleEnumerateFunctions")) return -1;
+    for (CUfunction f : fs) {
+        const char* name = nullptr;
+        if (cuFuncGetName(&name, f) != CUDA_SUCCESS || !name) continue;
+        if (std::strstr(name, "dicom_preprocess_kernel")) m.pre = f;
+        if (std::strstr(name, "filter_select_kernel")) m.filt = f;
+    }
+    if (!m.pre || !m.filt) {
+        g_err = "kernels not found in the cubin";
+        return -1;
+    }
+    g_mods.push_back(m);
+    return (int)g_mods.size() - 1;
+}
+
+// One strip through the reference kernels: input rows (rows * width_bytes,
+// DICOM little-endian samples when params is non-null), the prior row
+// (width_bytes, or null = zeros), params = the 40-byte DicomPixelParams or
+// null.  Writes the filtered strip (rows * (width_bytes + 1)) and, if
+// out_pre is non-null, the preprocessed rows.  0 on success.
+int rgr_run(int h, const unsigned char* input, const unsigned char* prior, int width_bytes, int bpp, int rows,
+            const void* params, unsigned char* out_filtered, unsigned char* out_pre)
+{
+    if (h < 0 || h >= (int)g_mods.size() || width_bytes < 1 || rows < 1) {
+        g_err = "bad arguments";
+        return 1;
+    }
+    if (!ck(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent")) return 2;
+    const Mod& m = g_mods[h];
+    const size_t in_bytes = (size_t)rows * width_bytes, out_bytes = (size_t)rows * (width_bytes + 1);
+    CUdeviceptr d_in = 0, d_prior = 0, d_sel = 0;
+    int rc = 0;
+    if (!ck(cuMemAlloc(&d_in, in_bytes + 256), "cuMemAlloc") || !ck(cuMemAlloc(&d_prior, width_bytes + 256), "cuMemAlloc") ||
+        !ck(cuMemAlloc(&d_sel, out_bytes + 256), "cuMemAlloc")) {
+        rc = 3;
+    } else {
+        std::vector<unsigned char> zeros(width_bytes, 0);
+        bool good = ck(cuMemcpyHtoD(d_in, input, in_bytes), "HtoD") &&
+                    ck(cuMemcpyHtoD(d_prior, prior ? prior : zeros.data(), width_bytes), "HtoD");
+        if (good && params) {
+            unsigned char p[40];
+            std::memcpy(p, params, 40);
+            int bits_alloc;
+            std::memcpy(&bits_alloc, p, 4);
+            int total = (int)(in_bytes / (size_t)(bits_alloc / 8));
+            void* args[] = {&d_in, &total, p};
+            good = ck(cuLaunchKernel(m.pre, (unsigned)((total + 255) / 256), 1, 1, 256, 1, 1, 0, nullptr, args, nullptr),
+                      "launch dicom_preprocess_kernel");
+        }
+        if (good) {
+            int wb = width_bytes, bp = bpp, nr = rows;
+            void* args[] = {&d_in, &d_prior, &d_sel, &wb, &bp, &nr};
+            good = ck(cuLaunchKernel(m.filt, (unsigned)rows, 1, 1, 256, 1, 1, 0, nullptr, args, nullptr),
+                      "launch filter_select_kernel") &&
+                   ck(cuCtxSynchronize(), "synchronize") && ck(cuMemcpyDtoH(out_filtered, d_sel, out_bytes), "DtoH") &&
+                   (!out_pre || ck(cuMemcpyDtoH(out_pre, d_in, in_bytes), "DtoH"));
+        }
+        if (!good) rc = 4;
+    }
+    if (d_in) cuMemFree(d_in);
+    if (d_prior) cuMemFree(d_prior);
+    if (d_sel) cuMemFree(d_sel);
+    return rc;
+}
+
+}  // extern "C"

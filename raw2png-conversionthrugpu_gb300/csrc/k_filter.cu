@@ -249,19 +249,32 @@ __host__ __device__ inline int slot_stride(int rb)
     return 16 + ((rb + 15) & ~15) + 16;
 }
 
-// Raw bytes staged per row by the bulk-copy path (0 when rows are not
-// 16-byte multiples and the plain-load path is used).
+// Raw bytes per row a bulk-copy tile stages (0 when rows are not 16-byte
+// multiples: plain loads then).
 __host__ __device__ inline int staged_pitch(int in_pitch) { return (in_pitch & 15) ? 0 : in_pitch; }
 
-// Rows per tile for a given dynamic shared-memory size: the most rows, up to
-// two passes of the warp groups, whose staging + (rows+1) slots fit.
-__host__ __device__ inline int tile_rows_for(int rb, int in_pitch, int smem, int lreg, int cap_rows)
+// Rows per tile for staging pitch sp in smem bytes of dynamic shared memory:
+// the most rows, up to cap_rows, whose staging + (rows+1) slots fit.
+__host__ __device__ inline int tile_rows_sp(int rb, int sp, int smem, int lreg, int cap_rows)
 {
     const int stride = slot_stride(rb);
-    const int sp = staged_pitch(in_pitch);
     for (int t = cap_rows; t >= 1; t--)
         if (lreg + t * sp + (t + 1) * stride <= smem) return t;
     return 0;
+}
+
+// Staging pitch actually used at a given shared-memory size: rows too wide to
+// stage even one row next to two ring slots are windowed from global memory
+// straight into the ring.  Host planning and the kernel both decide here.
+__host__ __device__ inline int staged_pitch_for(int rb, int in_pitch, int smem, int lreg)
+{
+    const int sp = staged_pitch(in_pitch);
+    return (sp && tile_rows_sp(rb, sp, smem, lreg, 1) >= 1) ? sp : 0;
+}
+
+__host__ __device__ inline int tile_rows_for(int rb, int in_pitch, int smem, int lreg, int cap_rows)
+{
+    return tile_rows_sp(rb, staged_pitch_for(rb, in_pitch, smem, lreg), smem, lreg, cap_rows);
 }
 
 __host__ __device__ inline int lut_region_bytes(int mode, int entries, int esize)
@@ -665,7 +678,7 @@ k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items,
         const int rpp = kFiltWarps / G;                     // rows per pass
         const int T = tile_rows_for(rb, d.in_pitch, smem_bytes, lreg, 2 * rpp);
         const int slots = T + 1;
-        const int sp = staged_pitch(d.in_pitch);
+        const int sp = staged_pitch_for(rb, d.in_pitch, smem_bytes, lreg);
         uint8_t* stage = smem + lreg;
         uint8_t* ring = stage + (size_t)T * sp;
         // bulk copies need a 16-byte aligned source; otherwise plain loads
@@ -833,12 +846,15 @@ int filter_smem_bytes(int rb, int in_pitch, int mode, int lut_entries, int lut_e
 {
     const int lreg = lut_region_bytes(mode, lut_entries, lut_esize);
     const int stride = slot_stride(rb);
-    const int sp = staged_pitch(in_pitch);
     const int rpp = kFiltWarps / warps_per_row(rb);
-    int t = tile_rows_for(rb, in_pitch, kFilterSmemTarget, lreg, 2 * rpp);
-    if (t == 0) t = tile_rows_for(rb, in_pitch, kFilterSmemCap, lreg, 2 * rpp);
+    int smem = kFilterSmemTarget;
+    int t = tile_rows_for(rb, in_pitch, smem, lreg, 2 * rpp);
+    if (t == 0) {
+        smem = kFilterSmemCap;
+        t = tile_rows_for(rb, in_pitch, smem, lreg, 2 * rpp);
+    }
     if (t == 0) return -1;
-    return lreg + t * sp + (t + 1) * stride;
+    return lreg + t * staged_pitch_for(rb, in_pitch, smem, lreg) + (t + 1) * stride;
 }
 
 int filter_tile_rows(int rb, int in_pitch, int smem, int lut_region)

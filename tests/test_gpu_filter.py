@@ -211,3 +211,56 @@ def test_strips_with_carried_last_row(engine, O, r2p, W, mode):
         last = new_last
         prior = last.ptr
     assert np.array_equal(np.concatenate(parts), want)
+
+
+def _golden():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gpu_filter_ref.npz"))
+
+
+_SPLIT = {1: (1, 1), 2: (1, 2), 3: (3, 1), 4: (4, 1), 6: (3, 2), 8: (4, 2)}
+
+
+def test_pinned_to_reference_kernels(engine, O, r2p):
+    """The fused window+filter kernel against outputs of the reference's own
+    dicom_preprocess_kernel + filter_select_kernel (src/gpu_filter.cu, IEEE
+    build) recorded on a GB300 (tests/golden/gen_gpu_golden.py)."""
+    d = _golden()
+    for k in range(int(d["n_flt"][0])):
+        wpx, rows, bpp = (int(x) for x in d["flt_%d_meta" % k])
+        prior = d["flt_%d_prior" % k]
+        pb = d["flt_%d_params" % k]
+        if pb.size:
+            p = r2p.DicomParams.from_buffer_copy(pb.tobytes())
+            bps = p.bits_allocated // 8
+            img = r2p.Image.make(wpx, rows, bpp // bps, bps, r2p.WINDOW_DICOM16, p)
+        else:
+            ch, bps = _SPLIT[bpp]
+            img = r2p.Image.make(wpx, rows, ch, bps, r2p.WINDOW_NONE)
+        got = engine.filter_image(img, d["flt_%d_in" % k], prior if prior.size else None)
+        assert np.array_equal(got, d["flt_%d_ieee" % k]), "case %d differs from the reference kernel" % k
+    # every stored value of each window parameter set, as an image
+    for k in range(int(d["n_a2"][0])):
+        p = r2p.DicomParams.from_buffer_copy(d["a2_%d_params" % k].tobytes())
+        ref = d["a2_%d_ieee" % k]
+        if p.bits_allocated == 16:
+            raw, w, h = np.arange(65536, dtype="<u2"), 256, 256
+        else:
+            raw, w, h = np.arange(256, dtype=np.uint8), 16, 16
+        bps = p.bits_allocated // 8
+        img = r2p.Image.make(w, h, 1, bps, r2p.WINDOW_DICOM16, p)
+        got = engine.filter_image(img, raw)
+        assert np.array_equal(got, O.filter_rows(ref, h, w * bps, bps)), "a2 set %d" % k
+
+
+@pytest.mark.parametrize("w,h,ch,bps,mode", [(17043, 6, 3, 2, 0), (45000, 5, 1, 2, 2), (13001, 4, 4, 2, 0)])
+def test_wide_rows(engine, O, r2p, w, h, ch, bps, mode):
+    """Rows too wide to stage next to the ring (>= 90 KB) take the plain-load
+    path; the reference handles 17043-pixel RGB16 rows."""
+    rng = np.random.default_rng(w)
+    raw = rng.integers(0, 4096, size=w * h * ch, dtype=np.uint16).astype("<u2" if mode else ">u2")
+    dp = r2p.DicomParams.make(16, 12, 11, 0, wc=2048.0, ww=4096.0) if mode else None
+    img = r2p.Image.make(w, h, ch, bps, mode, dp, level=1)
+    check(engine, O, r2p, img, raw)
+    from test_gpu_png import decode_and_check
+    decode_and_check(O, r2p, img, raw, engine.encode_png(img, raw))

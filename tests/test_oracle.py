@@ -112,3 +112,65 @@ def test_parse_png_rejects_bad_crc(O, W):
     png[40] ^= 1
     with pytest.raises(ValueError):
         O.parse_png(bytes(png))
+
+
+# --- pinned to the reference's own GPU kernels --------------------------------
+# tests/golden/gpu_filter_ref.npz holds outputs of dicom_preprocess_kernel and
+# filter_select_kernel (src/gpu_filter.cu) compiled from the reference sources
+# and run on a GB300 by tests/golden/gen_gpu_golden.py.  The "ieee" build uses
+# IEEE division and no FMA contraction; the "fm" build uses the reference's
+# own --use_fast_math (CMakeLists.txt:190).
+
+def gpu_golden():
+    return np.load(os.path.join(GOLDEN, "gpu_filter_ref.npz"))
+
+
+def a2_input(p):
+    """Every stored value of the parameter set's sample size, as raw bytes."""
+    if p.bits_allocated == 16:
+        return np.arange(65536, dtype="<u2").view(np.uint8)
+    return np.arange(256, dtype=np.uint8)
+
+
+def test_a2_pinned_to_reference_kernel(O):
+    d = gpu_golden()
+    for k in range(int(d["n_a2"][0])):
+        p = O.OrcParams.from_buffer_copy(d["a2_%d_params" % k].tobytes())
+        got = O.window_a2(a2_input(p), p)
+        assert np.array_equal(got, d["a2_%d_ieee" % k]), "a2 set %d differs from the reference kernel" % k
+        # The fast-math build differs only at a few truncation boundaries, by
+        # one output step: the known deviation of the reference's release build.
+        idx, val = d["a2_%d_fm_idx" % k], d["a2_%d_fm_val" % k]
+        assert idx.size <= 64
+        if p.bits_allocated == 16 and idx.size:
+            samples = np.unique(idx // 2)
+            ours = got.view(">u2")[samples].astype(np.int64)
+            fm = got.copy()
+            fm[idx] = val
+            theirs = fm.view(">u2")[samples].astype(np.int64)
+            assert np.all(np.abs(ours - theirs) == 1)
+
+
+def test_filter_pinned_to_reference_kernel(O):
+    d = gpu_golden()
+    seen_types = set()
+    for k in range(int(d["n_flt"][0])):
+        wpx, rows, bpp = (int(x) for x in d["flt_%d_meta" % k])
+        wb = wpx * bpp
+        inp = d["flt_%d_in" % k]
+        prior = d["flt_%d_prior" % k]
+        prior = prior if prior.size else None
+        pb = d["flt_%d_params" % k]
+        if pb.size:
+            p = O.OrcParams.from_buffer_copy(pb.tobytes())
+            win = O.window_a2(inp, p)
+            assert np.array_equal(win, d["flt_%d_pre_ieee" % k])
+        else:
+            win = inp
+        want = d["flt_%d_ieee" % k]
+        assert np.array_equal(O.filter_rows(win, rows, wb, bpp, prior), want), "filter case %d" % k
+        # the filter is integer: on the fast-math build's windowed rows it agrees too
+        assert np.array_equal(O.filter_rows(d["flt_%d_pre_fm" % k] if pb.size else inp, rows, wb, bpp, prior),
+                              d["flt_%d_fm" % k])
+        seen_types.update(int(t) for t in want.reshape(rows, wb + 1)[:, 0])
+    assert seen_types == {0, 1, 2, 3, 4}, "the recorded strips exercise every filter type"
