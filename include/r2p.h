@@ -277,6 +277,7 @@ int  r2p_event_create(void** ev);
 int  r2p_event_destroy(void* ev);
 int  r2p_event_record(void* ev, void* stream);
 int  r2p_event_elapsed_ms(void* ev_start, void* ev_end, float* ms);
+int  r2p_stream_wait_event(void* stream, void* ev);   /* later work on stream waits for ev */
 /* Stage timing: when enabled, each encode call records CUDA events on its
  * stream between its kernel launches; r2p_engine_stage_times() waits for
  * them, returns per-stage device milliseconds summed over the calls since the

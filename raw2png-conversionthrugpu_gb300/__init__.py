@@ -173,6 +173,7 @@ SIGNATURES = {
     "r2p_event_destroy": (ctypes.c_int, [_vp]),
     "r2p_event_record": (ctypes.c_int, [_vp, _vp]),
     "r2p_event_elapsed_ms": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(ctypes.c_float)]),
+    "r2p_stream_wait_event": (ctypes.c_int, [_vp, _vp]),
     "r2p_kernel_launch_count": (ctypes.c_uint64, []),
     "r2p_engine_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "r2p_batch_create": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Image), ctypes.POINTER(_vp),
@@ -317,6 +318,10 @@ class Stream:
 
     def sync(self):
         check(lib().r2p_stream_synchronize(self.ptr))
+
+    def wait(self, event):
+        """Later work on this stream waits for `event`."""
+        check(lib().r2p_stream_wait_event(self.ptr, event.ptr))
 
     def close(self):
         if getattr(self, "ptr", None):

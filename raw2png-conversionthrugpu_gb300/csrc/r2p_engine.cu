@@ -210,6 +210,10 @@ struct r2p_engine {
     int stage_idx = 0;
     cudaEvent_t done = nullptr;     // last kernel of the previous call
     bool have_done = false;
+    // stream of the host-buffer entry points: engines driven from different
+    // threads overlap their copies and kernels instead of sharing the
+    // legacy default stream
+    cudaStream_t hstream = nullptr;
     std::mutex mu;
     // stage timing (events between stage launches on the call's stream)
     bool timing = false;
@@ -548,6 +552,7 @@ int r2p_engine_create(int device, size_t hbm_budget, r2p_engine** out)
     if (ce == cudaSuccess) ce = cudaMalloc(&e->d_xpow, tab.size() * 4);
     if (ce == cudaSuccess) ce = cudaMemcpy(e->d_xpow, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->hstream, cudaStreamNonBlocking);
     for (int k = 0; k < r2p_engine::kStageRing && ce == cudaSuccess; k++)
         ce = cudaEventCreateWithFlags(&e->staged[k], cudaEventDisableTiming);
     if (ce != cudaSuccess) {
@@ -570,6 +575,10 @@ void r2p_engine_destroy(r2p_engine* e)
         if (e->staged[k]) cudaEventDestroy(e->staged[k]);
     }
     if (e->done) cudaEventDestroy(e->done);
+    if (e->hstream) {
+        cudaStreamSynchronize(e->hstream);
+        cudaStreamDestroy(e->hstream);
+    }
     for (auto& v : e->trec)
         for (auto ev : v) cudaEventDestroy(ev);
     delete e;
@@ -662,7 +671,7 @@ int r2p_encode_png(r2p_engine* e, const r2p_image* img, const void* h_pixels, vo
     cb.out = {nullptr};
     cb.out_cap = {bound};
     cb.out_len = {nullptr};
-    cudaStream_t s = 0;
+    cudaStream_t s = e->hstream;
     Prepared P;
     uint8_t* ext = nullptr;
     rc = prepare(e, plans, cb, raw_region + png_region + 256, s, P, &ext);
@@ -1044,6 +1053,11 @@ int r2p_event_destroy(void* ev)
 int r2p_event_record(void* ev, void* s)
 {
     R2P_CU(cudaEventRecord(static_cast<cudaEvent_t>(ev), static_cast<cudaStream_t>(s)), "cudaEventRecord");
+    return R2P_OK;
+}
+int r2p_stream_wait_event(void* s, void* ev)
+{
+    R2P_CU(cudaStreamWaitEvent(static_cast<cudaStream_t>(s), static_cast<cudaEvent_t>(ev), 0), "cudaStreamWaitEvent");
     return R2P_OK;
 }
 int r2p_event_elapsed_ms(void* a, void* b, float* ms)
