@@ -591,7 +591,7 @@ def main():
     ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c3", "c4"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--e2e-threads", type=int, default=4)
+    ap.add_argument("--e2e-threads", type=int, default=6)
     ap.add_argument("--streams", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
