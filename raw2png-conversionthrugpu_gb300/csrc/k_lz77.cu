@@ -77,38 +77,61 @@ __device__ __forceinline__ void lit_code(uint32_t b, uint32_t& v, int& n)
     else         { v = __brev(0x190u + b - 144u) >> 23; n = 9; }
 }
 
-// Length/distance pair -> packed bits (length code, extra, 5-bit distance code, extra).
-__device__ __forceinline__ void match_code(int len, int dist, uint32_t& v, int& n)
+// Code tables for matches (RFC 1951 3.2.5-3.2.6), built per CTA in shared
+// memory from the definitions below:
+//   length entry  [len - 3]           reversed code | bits << 8 | extra bits << 12 | base (len - 3) << 16
+//   distance entry [d < 256 ? d : 256 + (d >> 7)], d = distance - 1
+//                                     reversed 5-bit code | extra bits << 8 | base d << 12
+// (for d >= 256 a code has >= 7 extra bits, so d >> 7 fixes the code).
+constexpr int kLenTab = 256, kDistTab = 512;
+
+__device__ uint32_t len_entry(int len)
 {
-    int idx, lne, lex;
-    if (len == 258) { idx = 28; lne = 0; lex = 0; }
+    int idx, lne, base;
+    const int l = len - 3;
+    if (len == 258) { idx = 28; lne = 0; base = l; }
+    else if (l < 8) { idx = l; lne = 0; base = l; }
     else {
-        const int l = len - 3;
-        if (l < 8) { idx = l; lne = 0; lex = 0; }
-        else {
-            const int lg = 31 - __clz(l);
-            lne = lg - 2;
-            idx = 4 * lne + 4 + ((l >> lne) & 3);
-            lex = l & ((1 << lne) - 1);
-        }
+        const int lg = 31 - __clz(l);
+        lne = lg - 2;
+        idx = 4 * lne + 4 + ((l >> lne) & 3);
+        base = l & ~((1 << lne) - 1);
     }
     const int sym = 257 + idx;
     uint32_t code;
     int cl;
     if (sym <= 279) { code = __brev((uint32_t)(sym - 256)) >> 25; cl = 7; }
     else            { code = __brev((uint32_t)(0xC0 + sym - 280)) >> 24; cl = 8; }
-    const int d = dist - 1;
-    int dc, dne, dex;
-    if (d < 4) { dc = d; dne = 0; dex = 0; }
+    return code | ((uint32_t)cl << 8) | ((uint32_t)lne << 12) | ((uint32_t)base << 16);
+}
+
+__device__ uint32_t dist_entry(int i)
+{
+    const int d = i < 256 ? i : (i - 256) << 7;
+    int dc, dne, base;
+    if (d < 4) { dc = d; dne = 0; base = d; }
     else {
         const int lg = 31 - __clz(d);
         dne = lg - 1;
         dc = 2 * dne + 2 + ((d >> dne) & 1);
-        dex = d & ((1 << dne) - 1);
+        base = d & ~((1 << dne) - 1);
     }
-    v = code | ((uint32_t)lex << cl) | ((__brev((uint32_t)dc) >> 27) << (cl + lne)) |
-        ((uint32_t)dex << (cl + lne + 5));
-    n = cl + lne + 5 + dne;
+    return (__brev((uint32_t)dc) >> 27) | ((uint32_t)dne << 8) | ((uint32_t)base << 12);
+}
+
+// Length/distance pair -> packed bits (length code, extra, 5-bit distance code, extra).
+__device__ __forceinline__ void match_code(int len, int dist, const uint32_t* lt, const uint32_t* dt, uint32_t& v,
+                                           int& n)
+{
+    const uint32_t le = lt[len - 3];
+    const uint32_t cl = (le >> 8) & 15u, lne = (le >> 12) & 15u;
+    const uint32_t lex = (uint32_t)(len - 3) - (le >> 16);
+    const int d = dist - 1;
+    const uint32_t de = dt[d < 256 ? d : 256 + (d >> 7)];
+    const uint32_t dne = (de >> 8) & 15u;
+    const uint32_t dex = (uint32_t)d - (de >> 12);
+    v = (le & 0xFFu) | (lex << cl) | ((de & 31u) << (cl + lne)) | (dex << (cl + lne + 5));
+    n = (int)(cl + lne + 5 + dne);
 }
 
 // 4 bytes at i >= -3 with bytes at negative indices read as zero.
@@ -125,7 +148,8 @@ __device__ __forceinline__ uint32_t ld32z(const uint8_t* base, int i)
 // The thread keeps three sliding registers -- w (bytes p..p+3), the byte
 // before p, and wv (bytes p-rb1..p-rb1+3, the scanline above) -- so a literal
 // step reads one new byte per stream instead of two words per candidate.
-__device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb, uint16_t* tab, uint32_t* ob)
+__device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb, uint16_t* tab, uint32_t* ob,
+                               const uint32_t* lt, const uint32_t* dt)
 {
     const bool vert = rb1 > 1 && rb1 <= kMaxDist;
     uint64_t acc = 0;
@@ -169,7 +193,7 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb,
         uint32_t v;
         int nb;
         if (L >= 4) {
-            match_code(L, D, v, nb);
+            match_code(L, D, lt, dt, v, nb);
             p += L;
             w = ld32u(in, p);
             prev = in[p - 1];
@@ -235,7 +259,10 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     __shared__ uint32_t wsum[kLzWarps];
     __shared__ uint32_t s_info[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ uint32_t s_len[kLenTab], s_dist[kDistTab];
     build_crc_tables(ctab);
+    for (int i = threadIdx.x; i < kLenTab; i += kLzThreads) s_len[i] = len_entry(i + 3);
+    for (int i = threadIdx.x; i < kDistTab; i += kLzThreads) s_dist[i] = dist_entry(i);
     uint32_t* myout = outs + tid * lw;
 
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
@@ -273,7 +300,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         }
         // parse this thread's sub-range
         const int s = min(n, tid * sub), e = min(n, s + sub);
-        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, d.rb + 1, hb, mytab, myout) : 0u;
+        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, d.rb + 1, hb, mytab, myout, s_len, s_dist) : 0u;
         // CTA-wide exclusive scan of the bit counts
         uint32_t incl = nbits;
 #pragma unroll
