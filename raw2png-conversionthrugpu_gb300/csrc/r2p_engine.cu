@@ -307,13 +307,18 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
     P.slots_total = e->nsm * cps;
     uint64_t lut_total = 0, filt_total = 0;
     bool any11 = false;
-    for (int i = 0; i < n; i++) {
-        DevImage& d = plans[i].di;
-        if (P.smem > 0) {
+    // Row bands of the filter stage.  Tuned band heights suit batches of many
+    // images; when they would leave resident CTA slots idle (a lone image, a
+    // small batch) every image is split evenly instead.
+    auto plan_bands = [&](bool tuned) {
+        P.items.clear();
+        if (P.smem <= 0) return;
+        for (int i = 0; i < n; i++) {
+            const DevImage& d = plans[i].di;
             const int T = filter_tile_rows(d.rb, d.in_pitch, P.smem, plans[i].lreg);
             const uint64_t ntiles = (d.height + T - 1) / T;
             uint64_t band_rows;
-            if (plans[i].band_rows > 0) {
+            if (tuned && plans[i].band_rows > 0) {
                 band_rows = ((uint64_t)plans[i].band_rows + T - 1) / T * T;    // tuned, whole tiles
             } else {
                 // about one band per resident CTA (a lone image), split evenly;
@@ -326,6 +331,11 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
                 P.items.push_back(BandItem{(uint32_t)i, (uint32_t)r,
                                            (uint32_t)std::min<uint64_t>(d.height, r + band_rows)});
         }
+    };
+    plan_bands(true);
+    if (P.items.size() < (size_t)P.slots_total) plan_bands(false);
+    for (int i = 0; i < n; i++) {
+        DevImage& d = plans[i].di;
         d.blk0 = P.nblk;
         for (int k = 0; k < d.nblocks; k++) {
             BlockOut bo;
