@@ -209,7 +209,7 @@ def measure_c3(r2p, W, eng, stream, n=1000, reps=3):
     return res
 
 
-def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4, threads=4):
+def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4, threads=4, slots=4):
     """Served request stream: Poisson arrivals at fractions of the measured
     saturation rate; p50/p99 latency (submit -> PNG in host memory) and images/s,
     next to the plain per-image path (r2p_encode_png, one image at a time)."""
@@ -242,7 +242,7 @@ def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4,
         plain(img, pin)
     plain_ips = len(pool) / (time.perf_counter() - t0)
     eng.close()
-    sv = r2p.Server(0, hbm_budget=40 << 30, host_pool_bytes=8 << 30, max_inflight_batches=3)
+    sv = r2p.Server(0, hbm_budget=40 << 30, host_pool_bytes=8 << 30, max_inflight_batches=slots)
     try:
         with open(TUNING_JSON) as f:
             sv.set_tuning([tuple(c) for c in json.load(f)["classes"]])
@@ -278,14 +278,19 @@ def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4,
         wall = time.perf_counter() - start
         return lat, wall
 
-    # saturation: everything arrives at once
+    # saturation: everything arrives at once; median of three bursts of 2x the
+    # per-level count (one burst lasts only ~0.1 s)
     run([0.0] * 64)
-    sv.reset_stats()
-    lat, wall = run([0.0] * per_level)
-    sat = per_level / wall
-    st = sv.stats()
-    out = {"requests_per_level": per_level, "pool_images": len(pool), "mean_raw_bytes": int(mean_raw),
+    bursts = []
+    for _ in range(3):
+        sv.reset_stats()
+        lat, wall = run([0.0] * (2 * per_level))
+        bursts.append((2 * per_level / wall, sv.stats()))
+    sats = [b[0] for b in bursts]
+    sat, st = sorted(bursts, key=lambda b: b[0])[1]
+    out = {"requests_per_level": per_level, "pool_images": len(pool), "mean_raw_bytes": int(mean_raw), "slots": slots,
            "plain_images_per_s": round(plain_ips, 1), "saturation_images_per_s": round(sat, 1),
+           "saturation_runs_images_per_s": [round(x, 1) for x in sats],
            "saturation_vs_plain": round(sat / plain_ips, 2), "mean_batch_images_at_saturation":
            round(st["mean_batch_images"], 1), "levels": []}
     rng = random.Random(seed)
@@ -475,6 +480,12 @@ def run_ours(args):
     filt = zlib.decompress(png[41:len(png) - 16])      # IDAT data: zlib header .. Adler-32
     assert len(filt) == img.filtered_bytes, "benchmarked PNG does not inflate to the filtered size"
     comp_bytes = len(png)
+    # compressed size beside zlib on the same filtered scanlines (not timed;
+    # zlib-ng is not installed, the system zlib stands in)
+    sizes = {"ours_zlib_stream": len(png) - 57, "filtered_bytes": len(filt)}
+    for lv in (0, 1, 6):
+        sizes["zlib_level_%d" % lv] = len(zlib.compress(filt, lv))
+    sizes["zlib_version"] = zlib.ZLIB_RUNTIME_VERSION
     # e2e through the host entry point (r2p_encode_png) with pinned buffers:
     # `threads` workers, each with its own engine, take steps in turn, as the
     # reference's encode workers do; every step's pixels go host->device and
@@ -540,6 +551,7 @@ def run_ours(args):
                    "streams_per_gpu": S},
         "images_per_s": round(args.steps * world / (ms_max / 1e3), 2),
         "png_bytes": comp_bytes,
+        "compressed_vs_zlib": sizes,
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": img.raw_bytes,
                 "d2h_bytes_per_step": comp_bytes + 8,
                 "images_per_s": round(e2e_steps * world / e2e_s, 2),
@@ -556,7 +568,7 @@ def run_ours(args):
     line["config"]["tuning"] = tuning
     if not args.no_batched:
         line["batched_c3"] = measure_c3(r2p, W, eng, stream)
-        line["served_c4"] = measure_c4(r2p, W)
+        line["served_c4"] = measure_c4(r2p, W, slots=args.server_slots)
     if world == 1 and not args.no_cpu_baseline:
         from oracle import build_oracle, oracle as O
         build_oracle.build_oracle()
@@ -593,6 +605,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--e2e-threads", type=int, default=6)
     ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--server-slots", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -604,7 +617,8 @@ def main():
         import __graft_entry__ as g
         r2p = g.load_package()
         from raw2png_gb300 import workloads as W
-        print(json.dumps({"metric": "served images/s and p50/p99 latency", "served_c4": measure_c4(r2p, W)}),
+        print(json.dumps({"metric": "served images/s and p50/p99 latency",
+                          "served_c4": measure_c4(r2p, W, slots=args.server_slots)}),
               flush=True)
     else:
         run_ours(args)
