@@ -38,3 +38,18 @@ struct MemorySource : ImageSource {
     const DicomPixelParams* dicom_params() const override { return has_params_ ? &params_ : nullptr; }
     int read_strip(uint8_t* out, int max_rows) override;
 };
+
+// A TIFF file as a strip source (the reference's TiffSource, src/pipeline.cpp).
+struct TiffSource : ImageSource {
+    TiffSource() = default;
+    ~TiffSource() override;
+    TiffSource(const TiffSource&) = delete;
+    TiffSource& operator=(const TiffSource&) = delete;
+    bool open(const char* path);
+    const ImageInfo& info() const override { return info_; }
+    int read_strip(uint8_t* out, int max_rows) override;
+
+private:
+    struct TiffReader* r_ = nullptr;
+    ImageInfo info_;
+};

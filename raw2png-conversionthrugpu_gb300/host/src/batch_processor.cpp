@@ -24,6 +24,7 @@
 
 #include "dicom_loader.h"
 #include "file_type.h"
+#include "image_source.h"
 #include "host_common.h"
 
 namespace fs = std::filesystem;
@@ -135,6 +136,46 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
         return true;
     };
 
+    // a TIFF file: samples already in PNG order, no window
+    auto submit_tiff = [&](const std::string& path, const std::string& out, FileJob& job) -> bool {
+        TiffSource t;
+        if (!t.open(path.c_str())) return false;
+        const ImageInfo& info = t.info();
+        std::vector<uint8_t> px((size_t)info.width * info.height * info.bpp);
+        const size_t rb = (size_t)info.width * info.bpp;
+        for (int r = 0; r < (int)info.height;) {
+            const int n = t.read_strip(px.data() + (size_t)r * rb, (int)info.height - r);
+            if (n <= 0) return false;
+            r += n;
+        }
+        r2p_image img;
+        std::memset(&img, 0, sizeof(img));
+        img.width = info.width;
+        img.height = info.height;
+        img.channels = info.channels;
+        img.bytes_per_sample = info.bits_per_sample / 8;
+        img.window_mode = R2P_WINDOW_NONE;
+        img.level = level;
+        img.strip_height = cfg.strip_height > 0 ? cfg.strip_height : 1024;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] { return outstanding < kMaxOutstanding; });
+            outstanding++;
+        }
+        uint64_t tk = 0;
+        if (!r2p_host::ok(r2p_server_submit(srv, &img, px.data(), &tk), "r2p_server_submit")) {
+            std::lock_guard<std::mutex> lk(mu);
+            outstanding--;
+            cv.notify_all();
+            return false;
+        }
+        FrameJob fj;
+        fj.ticket = tk;
+        fj.out = out;
+        job.frames.push_back(fj);
+        return true;
+    };
+
     auto reader = [&]() {
         for (;;) {
             size_t i;
@@ -147,8 +188,10 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
             const std::string path = files[i].string();
             const std::string stem = files[i].stem().string();
             DicomSource src;
-            if (!is_dicom_file(path.c_str())) {
-                std::fprintf(stderr, "%s: TIFF and camera RAW input are not part of this build\n", path.c_str());
+            if (is_tiff_file(path.c_str())) {
+                job.ok = submit_tiff(path, (outdir / (stem + ".png")).string(), job);
+            } else if (!is_dicom_file(path.c_str())) {
+                std::fprintf(stderr, "%s: camera RAW input is not part of this build\n", path.c_str());
                 job.ok = false;
             } else if (!src.open(path.c_str())) {
                 job.ok = false;

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <filesystem>
 #include <string>
+#include <vector>
 
 #include "batch_processor.h"
 #include "dicom_loader.h"
@@ -23,7 +24,8 @@ static void usage(const char* prog)
 {
     std::fprintf(stderr,
                  "Usage: %s <input> <output> [options]\n"
-                 "  <input>  : DICOM file (uncompressed Implicit/Explicit VR Little Endian), or a folder\n"
+                 "  <input>  : DICOM file (uncompressed Implicit/Explicit VR Little Endian), an\n"
+                 "             uncompressed TIFF (.tif/.tiff), or a folder\n"
                  "  <output> : a .png file, or a folder with --all / folder input\n"
                  "  --all                every frame as <output>/slice_NNNN.png   (alias: -all)\n"
                  "  --frame N            export DICOM frame N (0-based)\n"
@@ -39,13 +41,29 @@ static void usage(const char* prog)
                  "  --strip-pipeline     run strips through gpu_filter + GpuDeflateBackend\n"
                  "  --idat-chunk N       IDAT chunks of at most N bytes (default: one IDAT)\n"
                  "  --device N           GPU ordinal\n"
-                 "  --probe              print the parsed DICOM header as JSON and exit\n"
+                 "  --probe              print the parsed DICOM/TIFF header as JSON and exit\n"
                  "  --bench-deflate [N]  GPU DEFLATE benchmark on N bytes (default 2400000)\n",
                  prog);
 }
 
 static int probe(const char* path)
 {
+    if (is_tiff_file(path)) {
+        TiffSource t;
+        if (!t.open(path)) return 1;
+        const ImageInfo& i = t.info();
+        std::vector<uint8_t> buf((size_t)i.width * i.bpp * 64);
+        uint64_t sum = 0;
+        int rows = 0, n;
+        while ((n = t.read_strip(buf.data(), 64)) > 0) {       // reads every strip
+            for (size_t k = 0; k < (size_t)n * i.width * i.bpp; k++) sum += buf[k];
+            rows += n;
+        }
+        std::printf("{\"format\": \"tiff\", \"width\": %u, \"height\": %u, \"channels\": %d, "
+                    "\"bits_per_sample\": %d, \"bpp\": %d, \"rows_read\": %d, \"byte_sum\": %llu}\n",
+                    i.width, i.height, i.channels, i.bits_per_sample, i.bpp, rows, (unsigned long long)sum);
+        return rows == (int)i.height ? 0 : 1;
+    }
     DicomSource s;
     if (!s.open(path)) return 1;
     const ImageInfo& i = s.info();

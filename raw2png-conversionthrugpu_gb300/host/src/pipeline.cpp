@@ -249,10 +249,18 @@ bool encode_source_to_bmp(ImageSource&, const char*)
     return false;
 }
 
-bool encode_tiff_to_png(const char* input_path, const char*, const PipelineConfig&)
+bool encode_tiff_to_png(const char* input_path, const char* output_path, const PipelineConfig& cfg)
 {
-    std::fprintf(stderr, "TIFF input is not part of this build: %s\n", input_path);
-    return false;
+    const auto t0 = std::chrono::steady_clock::now();
+    TiffSource src;
+    if (!src.open(input_path)) {
+        std::fprintf(stderr, "Cannot open TIFF: %s\n", input_path);
+        return false;
+    }
+    const bool good = encode_source_to_png(src, output_path, cfg);
+    pipeline_record_file_times(0, std::chrono::duration_cast<std::chrono::milliseconds>(
+                                      std::chrono::steady_clock::now() - t0).count());
+    return good;
 }
 
 bool encode_raw_to_png(const char* input_path, const char*, const PipelineConfig&)

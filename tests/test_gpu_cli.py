@@ -142,3 +142,36 @@ def test_reference_interfaces_from_cpp(cli, O, W, tmp_path, dicom, level):
     filt = np.frombuffer((tmp_path / "f.out").read_bytes(), np.uint8)
     assert np.array_equal(filt, O.filter_rows(win, h, w * bpp, bpp)), "filtered strips differ from the oracle"
     assert zlib.decompress((tmp_path / "z.out").read_bytes()) == filt.tobytes()
+
+
+import tiff_files as T  # noqa: E402
+
+
+@pytest.mark.parametrize("order,photo", [("II", None), ("MM", None), ("II", 0)])
+def test_tiff_to_png(cli, O, tmp_path, order, photo):
+    """TIFF in the reference's loader conventions: 16-bit samples
+    big-endian in the PNG, MINISWHITE inverted (src/image_loader.cpp:200-212)."""
+    rng = np.random.default_rng(11)
+    img = (rng.integers(0, 4096, size=(57, 83, 3)) * 16).astype(np.uint16)
+    if photo == 0:
+        img = img[..., 0]
+    f = tmp_path / "rgb.tif"
+    T.write_tiff(f, img, order=order, rows_per_strip=9, photometric=photo)
+    out = tmp_path / "rgb.png"
+    run(cli, f, out, "--level", 1)
+    check_png(O, out, T.expected_png_bytes(img, photo), 16, 2 if img.ndim == 3 else 0)
+
+
+def test_folder_with_tiff(cli, O, W, tmp_path):
+    src = tmp_path / "in"
+    src.mkdir()
+    img = np.random.default_rng(12).integers(0, 256, size=(40, 50, 3), dtype=np.uint8)
+    T.write_tiff(src / "photo.tif", img, rows_per_strip=16)
+    px = W.ct_phantom(30, 128, 96)
+    D.write_dicom(src / "ct.dcm", px, slope=1.0, intercept=-1024.0, wc=40.0, ww=400.0)
+    dst = tmp_path / "out"
+    out = run(cli, src, dst, "--level", 1)
+    assert "2/2 OK" in out
+    check_png(O, dst / "photo.png", T.expected_png_bytes(img), 8, 2)
+    want, _ = O.window8(px.view(np.uint8), O.make_params(16, 12, 11, 0, slope=1.0, intercept=-1024.0, wc=40.0, ww=400.0))
+    check_png(O, dst / "ct.png", want, 8, 0)

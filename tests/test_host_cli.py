@@ -113,3 +113,32 @@ def test_cli_usage_and_unknown_option(cli, tmp_path):
     assert r.returncode == 1 and "--strip-height" in r.stderr and "--level" in r.stderr
     r = subprocess.run([cli, "a.dcm", "b.png", "--bogus"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "Unknown option" in r.stderr
+
+
+# --- TIFF ---------------------------------------------------------------------
+import tiff_files as T  # noqa: E402
+
+
+@pytest.mark.parametrize("order", ["II", "MM"])
+@pytest.mark.parametrize("shape,dtype", [((33, 41), np.uint16), ((20, 17, 3), np.uint8), ((9, 11, 4), np.uint16)])
+def test_tiff_probe(cli, tmp_path, order, shape, dtype):
+    rng = np.random.default_rng(7)
+    img = rng.integers(0, np.iinfo(dtype).max + 1, size=shape, dtype=dtype)
+    f = tmp_path / "a.tif"
+    T.write_tiff(f, img, order=order, rows_per_strip=5)
+    r = subprocess.run([cli, str(f), "--probe"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    h = json.loads(r.stdout)
+    ch = shape[2] if len(shape) == 3 else 1
+    assert (h["width"], h["height"], h["channels"], h["bits_per_sample"]) == (shape[1], shape[0], ch, 8 * img.itemsize)
+    assert h["rows_read"] == shape[0]
+    assert h["byte_sum"] == int(T.expected_png_bytes(img).astype(np.uint64).sum())
+
+
+def test_tiff_refusals(cli, tmp_path):
+    img = np.zeros((8, 8), np.uint16)
+    for kw, msg in (({"compression": 5}, "compressed"), ({"tiled": True}, "tiled")):
+        f = tmp_path / ("x%s.tif" % msg)
+        T.write_tiff(f, img, **kw)
+        r = subprocess.run([cli, str(f), "--probe"], capture_output=True, text=True, timeout=60)
+        assert r.returncode != 0 and msg in r.stderr
