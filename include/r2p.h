@@ -149,6 +149,18 @@ typedef struct r2p_tuning {
 int r2p_engine_set_tuning(r2p_engine* eng, int n, const r2p_tuning* classes);
 int r2p_engine_get_tuning(r2p_engine* eng, int cap, r2p_tuning* out, int* n);
 
+/* Encode n images from host memory (any mix of sizes and modes), each as by
+ * r2p_encode_png, with the copies and kernels of up to R2P_MANY_SLOTS images
+ * in flight at once (helper engines, each with its own arena and stream):
+ * one host thread keeps the GPU busy across images.  Pinned host buffers let
+ * copies overlap; pageable ones are correct but serialise.  statuses (may be
+ * NULL) receives each image's status; returns R2P_OK or the first failure.
+ * The reference encodes images one at a time per worker thread
+ * (src/batch_processor.cpp:482-737, src/pipeline.cpp:1571). */
+#define R2P_MANY_SLOTS 4
+int r2p_encode_png_many(r2p_engine* eng, int n, const r2p_image* imgs, const void* const* h_pixels,
+                        void* const* h_pngs, const size_t* png_caps, size_t* png_lens, int* statuses);
+
 /* Stage entry point: window + adaptive filter of a whole image into
  * height*(row_bytes+1) filtered scanline bytes on the device.  d_prior (may
  * be NULL = zeros) is the windowed row above row 0.  Replaces

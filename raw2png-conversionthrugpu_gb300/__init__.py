@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libr2p.so")
 
 OK, EINVAL, ENOMEM, EBUDGET, ECUDA, ETIMEOUT, ENOSPC, ECANCELED, ENOTFOUND = range(9)
 WINDOW_NONE, WINDOW_SWAP16, WINDOW_DICOM16, WINDOW_BATCH8 = range(4)
+MANY_SLOTS = 4          # R2P_MANY_SLOTS: images in flight in Engine.encode_png_many
 BLOCK64 = 65520
 BLOCK32 = 32752
 
@@ -147,6 +148,9 @@ SIGNATURES = {
     "r2p_png_bound": (_sz, [ctypes.POINTER(Image)]),
     "r2p_encode_png": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _sz, ctypes.POINTER(_sz)]),
     "r2p_encode_png_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _sz, _vp, _vp]),
+    "r2p_encode_png_many": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Image), ctypes.POINTER(_vp),
+                                           ctypes.POINTER(_vp), ctypes.POINTER(_sz), ctypes.POINTER(_sz),
+                                           ctypes.POINTER(ctypes.c_int)]),
     "r2p_encode_batch_device": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Image), ctypes.POINTER(_vp),
                                                ctypes.POINTER(_vp), ctypes.POINTER(_sz), _vp, _vp]),
     "r2p_window_filter_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp]),
@@ -390,6 +394,42 @@ class Engine:
         n = _sz()
         check(lib().r2p_encode_png(self.h, ctypes.byref(img), px.ctypes.data, out.ctypes.data, cap, ctypes.byref(n)))
         return out[:n.value].tobytes()
+
+    def encode_png_many(self, imgs, inputs, outputs=None):
+        """Host images -> PNGs with up to MANY_SLOTS images in flight
+        (r2p_encode_png_many).  inputs: numpy arrays or PinnedBuffers;
+        outputs: optional PinnedBuffers (>= png_bound each; may repeat with a
+        period that is a multiple of MANY_SLOTS).  Returns (statuses,
+        PNG bytes, or PNG lengths when outputs are given)."""
+        n = len(imgs)
+        arr_imgs = (Image * n)(*imgs)
+        keep = []
+        ptr_in = (_vp * n)()
+        for i, x in enumerate(inputs):
+            if isinstance(x, PinnedBuffer):
+                ptr_in[i] = x.ptr
+            else:
+                a = np.ascontiguousarray(x).view(np.uint8).reshape(-1)
+                keep.append(a)
+                ptr_in[i] = a.ctypes.data
+        caps = (_sz * n)(*[png_bound(im) for im in imgs])
+        ptr_out = (_vp * n)()
+        own = None
+        if outputs is None:
+            own = [np.empty(caps[i], np.uint8) for i in range(n)]
+            for i in range(n):
+                ptr_out[i] = own[i].ctypes.data
+        else:
+            for i, o in enumerate(outputs):
+                ptr_out[i] = o.ptr
+                caps[i] = o.nbytes
+        lens = (_sz * n)()
+        sts = (ctypes.c_int * n)()
+        lib().r2p_encode_png_many(self.h, n, arr_imgs, ptr_in, ptr_out, caps, lens, sts)
+        statuses = list(sts)
+        if own is None:
+            return statuses, [int(lens[i]) for i in range(n)]
+        return statuses, [own[i][:lens[i]].tobytes() if statuses[i] == OK else None for i in range(n)]
 
     def encode_png_device(self, img, d_pixels, d_png, png_cap, d_len, stream=None):
         check(lib().r2p_encode_png_device(self.h, ctypes.byref(img), d_pixels, d_png, png_cap, d_len, _sp(stream)))

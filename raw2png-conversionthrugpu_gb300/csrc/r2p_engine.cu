@@ -214,6 +214,11 @@ struct r2p_engine {
     // threads overlap their copies and kernels instead of sharing the
     // legacy default stream
     cudaStream_t hstream = nullptr;
+    // r2p_encode_png_many: helper engines (own arena and stream each), the
+    // pinned length words they read back, and their events
+    std::vector<r2p_engine*> helpers;
+    uint64_t* many_lens = nullptr;
+    cudaEvent_t many_ev[R2P_MANY_SLOTS] = {};
     std::mutex mu;
     // stage timing (events between stage launches on the call's stream)
     bool timing = false;
@@ -589,6 +594,10 @@ void r2p_engine_destroy(r2p_engine* e)
         cudaStreamSynchronize(e->hstream);
         cudaStreamDestroy(e->hstream);
     }
+    for (r2p_engine* h : e->helpers) r2p_engine_destroy(h);
+    for (auto ev : e->many_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (e->many_lens) cudaFreeHost(e->many_lens);
     for (auto& v : e->trec)
         for (auto ev : v) cudaEventDestroy(ev);
     delete e;
@@ -708,6 +717,135 @@ int r2p_encode_png(r2p_engine* e, const r2p_image* img, const void* h_pixels, vo
     R2P_CU(cudaMemcpyAsync(h_png, d_png, (size_t)len, cudaMemcpyDeviceToHost, s), "png download");
     R2P_CU(cudaStreamSynchronize(s), "sync");
     return R2P_OK;
+}
+
+// Extra arena bytes of one host-buffer image: raw pixels, the PNG, its length word.
+static size_t host_call_extra(const ImgPlan& p)
+{
+    return align_up((size_t)p.raw_bytes + 16, 256) + align_up((size_t)p.png_bound, 256) + 256;
+}
+
+int r2p_encode_png_many(r2p_engine* e, int n, const r2p_image* imgs, const void* const* h_pixels,
+                        void* const* h_pngs, const size_t* png_caps, size_t* png_lens, int* statuses)
+{
+    if (!e || n < 0 || (n > 0 && (!imgs || !h_pixels || !h_pngs || !png_caps || !png_lens)))
+        return set_err(R2P_EINVAL, "NULL argument");
+    if (n == 0) return R2P_OK;
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    const int K = R2P_MANY_SLOTS;
+    while ((int)e->helpers.size() < K) {
+        r2p_engine* h = nullptr;
+        rc = r2p_engine_create(e->device, e->budget, &h);
+        if (rc) return rc;
+        e->helpers.push_back(h);
+    }
+    if (!e->many_lens) R2P_CU(cudaMallocHost(&e->many_lens, sizeof(uint64_t) * K), "cudaMallocHost");
+    for (int k = 0; k < K; k++)
+        if (!e->many_ev[k]) R2P_CU(cudaEventCreateWithFlags(&e->many_ev[k], cudaEventDisableTiming), "event");
+    // plan every image first and size the helpers' arenas once: an arena must
+    // not move while an earlier image's PNG download from it is queued
+    std::vector<ImgPlan> plans(n);
+    size_t need = 0;
+    int first_err = R2P_OK;
+    std::vector<int> st(n, R2P_OK);
+    for (int i = 0; i < n; i++) {
+        st[i] = plan_image(imgs[i], 0, plans[i], e->tuning);
+        if (st[i]) {
+            if (!first_err) first_err = st[i];
+            continue;
+        }
+        std::vector<ImgPlan> one{plans[i]};
+        CallBuffers cb;
+        cb.raw = {nullptr}; cb.filt = {nullptr}; cb.prior = {nullptr}; cb.out = {nullptr};
+        cb.out_cap = {plans[i].png_bound}; cb.out_len = {nullptr};
+        Prepared P;
+        plan_work(e, one, cb, host_call_extra(plans[i]), P);
+        need = std::max(need, P.total);
+    }
+    for (r2p_engine* h : e->helpers) {
+        std::lock_guard<std::mutex> hl(h->mu);
+        h->tuning = e->tuning;
+        rc = bind(h);
+        if (!rc) rc = ensure_arena(h, need);
+        if (rc) return rc;
+    }
+    struct Inflight {
+        int img = -1;
+        uint8_t* d_png = nullptr;
+    };
+    std::vector<Inflight> fl(K);
+    // the PNG of slot k's image: its length is on the host once the event fired
+    auto finish = [&](int k) {
+        const int j = fl[k].img;
+        fl[k].img = -1;
+        r2p_engine* h = e->helpers[k];
+        const cudaError_t ce = cudaEventSynchronize(e->many_ev[k]);
+        if (ce != cudaSuccess) {
+            st[j] = cuda_err(ce, "length wait");
+            return;
+        }
+        const uint64_t len = e->many_lens[k];
+        if (len >> 63) {
+            st[j] = set_err((int)(len & 0xFF), "device reported an error");
+            return;
+        }
+        png_lens[j] = (size_t)len;
+        if (len > png_caps[j]) {
+            st[j] = set_err(R2P_ENOSPC, "png_cap too small for the encoded PNG");
+            return;
+        }
+        const cudaError_t c2 = cudaMemcpyAsync(h_pngs[j], fl[k].d_png, (size_t)len, cudaMemcpyDeviceToHost, h->hstream);
+        if (c2 != cudaSuccess) st[j] = cuda_err(c2, "png download");
+    };
+    auto enqueue = [&](int k, int i) -> int {
+        r2p_engine* h = e->helpers[k];
+        std::lock_guard<std::mutex> hl(h->mu);
+        std::vector<ImgPlan> one{plans[i]};
+        const size_t raw_bytes = (size_t)plans[i].raw_bytes, bound = (size_t)plans[i].png_bound;
+        const size_t raw_region = align_up(raw_bytes + 16, 256), png_region = align_up(bound, 256);
+        CallBuffers cb;
+        cb.raw = {nullptr}; cb.filt = {nullptr}; cb.prior = {nullptr}; cb.out = {nullptr};
+        cb.out_cap = {bound}; cb.out_len = {nullptr};
+        cudaStream_t s = h->hstream;
+        Prepared P;
+        uint8_t* ext = nullptr;
+        int r = prepare(h, one, cb, host_call_extra(plans[i]), s, P, &ext);
+        if (r) return r;
+        uint8_t* d_raw = ext;
+        uint8_t* d_png = ext + raw_region;
+        uint64_t* d_len = reinterpret_cast<uint64_t*>(d_png + png_region);
+        cb.raw = {d_raw}; cb.out = {d_png}; cb.out_len = {d_len};
+        R2P_CU(cudaMemcpyAsync(d_raw, h_pixels[i], raw_bytes, cudaMemcpyHostToDevice, s), "pixel upload");
+        r = launch(h, one, cb, P, ST_ALL, s);
+        if (r) return r;
+        R2P_CU(cudaMemcpyAsync(e->many_lens + k, d_len, sizeof(uint64_t), cudaMemcpyDeviceToHost, s), "length");
+        R2P_CU(cudaEventRecord(e->many_ev[k], s), "event");
+        fl[k].img = i;
+        fl[k].d_png = d_png;
+        return R2P_OK;
+    };
+    int slot = 0;
+    for (int i = 0; i < n; i++) {
+        if (st[i]) continue;
+        const int k = slot;
+        slot = (slot + 1) % K;
+        if (fl[k].img >= 0) finish(k);
+        const int r = enqueue(k, i);
+        if (r) st[i] = r;
+    }
+    for (int k = 0; k < K; k++)
+        if (fl[k].img >= 0) finish(k);
+    for (r2p_engine* h : e->helpers) {
+        const cudaError_t ce = cudaStreamSynchronize(h->hstream);
+        if (ce != cudaSuccess && !first_err) first_err = cuda_err(ce, "sync");
+    }
+    for (int i = 0; i < n; i++) {
+        if (statuses) statuses[i] = st[i];
+        if (st[i] && !first_err) first_err = st[i];
+    }
+    return first_err ? set_err(first_err, "at least one image failed") : R2P_OK;
 }
 
 int r2p_window_filter_device(r2p_engine* e, const r2p_image* img, const void* d_pixels, const void* d_prior,

@@ -108,3 +108,41 @@ def test_checksums_all_ones_and_unaligned(engine, r2p):
     assert int(res.download(4).view(np.uint32)[0]) == zlib.crc32(ref)
     engine.adler32_device(buf.ptr + 3, 123457, res.ptr)
     assert int(res.download(4).view(np.uint32)[0]) == zlib.adler32(ref)
+
+
+def test_encode_png_many_matches_single_calls(engine, O, r2p, W):
+    """r2p_encode_png_many keeps several images in flight; each result equals
+    r2p_encode_png of the same image, and one bad image fails alone."""
+    specs = [(300, 200, 1, 1), (640, 480, 2, 1), (128, 96, 1, 0), (1024, 700, 2, 6), (77, 33, 1, 1),
+             (512, 512, 2, 0), (900, 300, 1, 1), (256, 256, 2, 1), (333, 444, 1, 1)]
+    imgs, raws = [], []
+    for i, (w, h, kind, level) in enumerate(specs):
+        raw = W.ct_phantom(60 + i, w, h)
+        img = (W.image_ct8 if kind == 1 else W.image_ct16)(w, h, 40.0 + i, 400.0, level=level)
+        imgs.append(img)
+        raws.append(raw)
+    bad = r2p.Image.make(64, 64, 2, 2, r2p.WINDOW_NONE)          # 2 channels: rejected
+    imgs.insert(4, bad)
+    raws.insert(4, np.zeros(64 * 64 * 2, np.uint16))
+    sts, pngs = engine.encode_png_many(imgs, raws)
+    assert sts[4] == r2p.EINVAL and pngs[4] is None
+    for i, (img, raw) in enumerate(zip(imgs, raws)):
+        if i == 4:
+            continue
+        assert sts[i] == r2p.OK
+        assert pngs[i] == engine.encode_png(img, raw), "image %d differs from the single call" % i
+        decode_and_check(O, r2p, img, raw, pngs[i])
+    # pinned inputs and a ring of pinned outputs of period 2 * MANY_SLOTS
+    pins = []
+    for raw in raws[:4]:
+        p = r2p.PinnedBuffer(raw.nbytes)
+        p.array[:] = raw.view(np.uint8).reshape(-1)
+        pins.append(p)
+    ring = [r2p.PinnedBuffer(max(r2p.png_bound(im) for im in imgs[:4])) for _ in range(2 * r2p.MANY_SLOTS)]
+    n = 3 * len(ring)
+    sts, lens = engine.encode_png_many([imgs[i % 4] for i in range(n)], [pins[i % 4] for i in range(n)],
+                                       [ring[i % len(ring)] for i in range(n)])
+    assert all(st == r2p.OK for st in sts)
+    for i in range(n - len(ring), n):                            # the last image written to each buffer
+        got = bytes(ring[i % len(ring)].array[:lens[i]])
+        assert got == engine.encode_png(imgs[i % 4], raws[i % 4])
