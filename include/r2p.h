@@ -136,8 +136,8 @@ void   r2p_batch_destroy(r2p_batch* b);
 /* Size-class tuning: per class of raw image bytes (sorted, the last class
  * takes everything larger), the DEFLATE block size used when an image's
  * block_size is 0, the filter's rows per work item (0 = from occupancy) and
- * the LZ77 hash-table size (2^10 or 2^11 entries per warp; one per launch,
- * the value most blocks of the launch were tuned for).  Set from the
+ * the LZ77 hash-table bits per image (9 or 10: 2^9 or 2^10 entries per
+ * warp).  Set from the
  * autotuner's table; n = 0 restores the built-in one.  Replaces the fixed
  * strip-height/pool-size defaults (src/main.cpp:165-170, src/pipeline.cpp:1587). */
 typedef struct r2p_tuning {

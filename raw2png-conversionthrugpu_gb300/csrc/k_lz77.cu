@@ -8,21 +8,23 @@
 // Only inflate-equality is required of the compressed bytes.
 //
 // Design.  One CTA per DEFLATE block (<= 65520 filtered bytes, staged in
-// shared memory).  Every one of the CTA's 512 threads parses its own
-// 132-byte sub-range of the block sequentially -- a greedy LZ77 with three
-// candidates per position: distance 1 (a run), the same column one scanline
-// up, and the head of a 4-byte hash table shared by the 32 lanes of a warp
-// (seeded from the 4 KB before the warp's range).  Matches may reach any
-// earlier byte of the block within 32 KB but end inside the thread's
-// sub-range, and are extended by word compares.  Each thread packs its
-// fixed-Huffman codes LSB-first into a 64-bit register and spills whole words
-// to a private shared-memory buffer (an odd word stride keeps the 32 lanes on
-// distinct banks), so no atomics are needed while parsing.  A CTA-wide scan
-// of the per-thread bit counts places the 512 bitstreams behind the 3-bit
-// block header; an end-of-block code and an empty stored block byte-align the
-// output, so blocks are independent and join by plain concatenation.  A block
-// whose Huffman form would not be smaller is emitted as a stored block.  The
-// CTA also leaves the block's Adler-32 sums (input) and CRC-32 (output).
+// shared memory).  Every one of the CTA's 1024 threads parses its own
+// 68-byte sub-range of the block sequentially (32 warps per SM: the parse is
+// latency-bound, so the warps hide each other's dependency chains) -- a
+// greedy LZ77 with three candidates per position: distance 1 (a run), the
+// same column one scanline up, and the head of a 4-byte hash table shared by
+// the 32 lanes of a warp (seeded from the ~2 KB before the warp's range).
+// Matches may reach any earlier byte of the block within 32 KB but end inside
+// the thread's sub-range, and are extended by word compares.  Each thread
+// packs its fixed-Huffman codes LSB-first into a 64-bit register (codes from
+// per-CTA tables) and spills whole words to a private shared-memory buffer
+// (an odd word stride keeps the 32 lanes on distinct banks), so no atomics
+// are needed while parsing.  A CTA-wide scan of the per-thread bit counts
+// places the bitstreams behind the 3-bit block header; an end-of-block code
+// and an empty stored block byte-align the output, so blocks are independent
+// and join by plain concatenation.  A block whose Huffman form would not be
+// smaller is emitted as a stored block.  The CTA also leaves the block's
+// Adler-32 sums (input) and CRC-32 (output).
 #include <cuda_runtime.h>
 
 #include "k_deflate.cuh"
@@ -30,7 +32,7 @@
 
 namespace r2p {
 
-constexpr int kLzWarps = 16;
+constexpr int kLzWarps = 32;
 constexpr int kLzThreads = kLzWarps * 32;
 constexpr int kPrefill = 4096;        // history bytes hashed before a warp's range
 constexpr int kMaxDist = 32768;
@@ -45,7 +47,7 @@ __host__ __device__ inline int lz_sub_bytes(int block_size)
     const int w = ((block_size + kLzThreads - 1) / kLzThreads + 3) >> 2;
     return 4 * (w | 1);
 }
-__host__ __device__ inline int lz_lane_words(int block_size) { return ((lz_sub_bytes(block_size) * 9 + 31) / 32 + 2) | 1; }
+__host__ __device__ inline int lz_lane_words(int block_size) { return ((lz_sub_bytes(block_size) * 9 + 31) / 32) | 1; }
 __host__ __device__ inline int lz_in_bytes(int block_size) { return ((block_size + 15) & ~15) + 64; }
 
 static int lz_smem_bytes(int block_size, int hash_bits)
@@ -67,8 +69,9 @@ __device__ __forceinline__ uint32_t ld32u(const uint8_t* base, int p)
 // Multiplicative hash of 4 bytes to hb bits.
 __device__ __forceinline__ uint32_t hash4(uint32_t v, int hb) { return (v * 2654435761u) >> (32 - hb); }
 
-// An image's hash table bits: 10 or 11.
-__device__ __forceinline__ int lz_hash_bits(const DevImage& d) { return d.hash_bits == 10 ? 10 : 11; }
+// An image's hash table bits: 9 or 10 (32 warps of 2^10 u16 entries fit beside
+// a 64 KB block; 11 bits would not).
+__device__ __forceinline__ int lz_hash_bits(const DevImage& d) { return d.hash_bits == 9 ? 9 : 10; }
 
 // Fixed-Huffman code of a literal byte: reversed code and its length.
 __device__ __forceinline__ void lit_code(uint32_t b, uint32_t& v, int& n)
@@ -243,7 +246,7 @@ __device__ void cta_adler_sums(const uint8_t* buf, int n, uint32_t& s1_out, uint
     s2_out = cta_sum64<NT>(s2, red64);
 }
 
-__global__ void __launch_bounds__(kLzThreads, 2)
+__global__ void __launch_bounds__(kLzThreads, 1)
 k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int max_block,
               uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
 {
@@ -292,7 +295,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         // seed the warp's table from the bytes before its range, oldest first
         const int sub = lz_sub_bytes(n);
         const int ws0 = min(n, warp * 32 * sub);
-        const int prefill = min(kPrefill, d.block_size >> 4);          // ~one warp range of history
+        const int prefill = min(kPrefill, d.block_size / kLzWarps);    // ~one warp range of history
         for (int q0 = max(0, ws0 - prefill); q0 < ws0; q0 += 32) {
             const int q = q0 + lane;
             if (q < ws0 && q + 4 <= n) mytab[hash4(ld32u(in, q), hb)] = (uint16_t)(q + 1);
@@ -374,11 +377,11 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     }
 }
 
-// hash_bits: the largest table size among the launch's images (10 or 11).
+// hash_bits: the largest table size among the launch's images (9 or 10).
 cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
                         uint64_t slot_bytes, const uint32_t* xpow, int grid, int hash_bits, cudaStream_t s)
 {
-    const int smem = lz_smem_bytes(max_block, hash_bits == 10 ? 10 : 11);
+    const int smem = lz_smem_bytes(max_block, hash_bits == 9 ? 9 : 10);
     cudaError_t e = cudaFuncSetAttribute(k_lz77_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     k_lz77_blocks<<<grid, kLzThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);

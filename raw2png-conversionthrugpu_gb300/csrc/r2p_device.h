@@ -46,7 +46,7 @@ struct DevImage {
     // DEFLATE / PNG
     int32_t level;
     int32_t block_size;             // filtered bytes per DEFLATE block
-    int32_t hash_bits;              // LZ77 hash table bits (10 or 11; other values mean 11)
+    int32_t hash_bits;              // LZ77 hash table bits (9 or 10; other values mean 10)
     int32_t nblocks;
     uint32_t blk0;                  // first global block index of this image
     int32_t out_kind;               // 0 = PNG file, 1 = bare zlib stream, 2 = raw DEFLATE

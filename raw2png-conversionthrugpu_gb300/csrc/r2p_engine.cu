@@ -90,12 +90,12 @@ struct ImgPlan {
     int smem = 0;      // filter smem wanted
     int lreg = 0;      // worst-case LUT region
     int band_rows = 0; // rows per filter work item (0 = from occupancy)
-    int hash_bits = 11;
+    int hash_bits = 10;
 };
 
 // Built-in size-class table (every class: 64 KiB blocks, bands from
 // occupancy, 2^11-entry LZ77 hash tables); engines may load an autotuned one.
-static const std::vector<r2p_tuning> kDefaultTuning = {{~0ull, kBlock64, 0, 11}};
+static const std::vector<r2p_tuning> kDefaultTuning = {{~0ull, kBlock64, 0, 10}};
 
 static const r2p_tuning& tune_for(const std::vector<r2p_tuning>& t, uint64_t raw_bytes)
 {
@@ -298,7 +298,7 @@ struct Prepared {
     uint64_t slot = 0;
     size_t o_img = 0, o_items = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0, o_extra = 0;
     size_t total = 0;
-    int hash_bits = 11;
+    int hash_bits = 10;
     int stage_slot = 0;
 };
 
@@ -311,7 +311,7 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
     const int cps = P.smem > 0 ? filter_ctas_per_sm(P.smem) : 1;
     P.slots_total = e->nsm * cps;
     uint64_t lut_total = 0, filt_total = 0;
-    bool any11 = false;
+    bool any10 = false;
     // Row bands of the filter stage.  Tuned band heights suit batches of many
     // images; when they would leave resident CTA slots idle (a lone image, a
     // small batch) every image is split evenly instead.
@@ -353,13 +353,13 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
         P.nblk += (uint32_t)d.nblocks;
         P.max_block = std::max(P.max_block, d.block_size);
         if (d.level == 0) P.any_stored = true; else P.any_lz = true;
-        d.hash_bits = plans[i].hash_bits == 10 ? 10 : 11;
-        if (d.level > 0 && d.hash_bits == 11) any11 = true;
+        d.hash_bits = plans[i].hash_bits == 9 ? 9 : 10;
+        if (d.level > 0 && d.hash_bits == 10) any10 = true;
         lut_total += plans[i].lut_cap;
         if (!cb.filt[i]) filt_total += align_up(d.filt_bytes + 64, 256);
     }
     // one hash-table size per launch: the one most blocks were tuned for
-    P.hash_bits = any11 ? 11 : 10;     // LZ77 tables sized for the largest; each block uses its image's
+    P.hash_bits = any10 ? 10 : 9;      // LZ77 tables sized for the largest; each block uses its image's
     P.slot = P.any_lz ? lz77_slot_bytes(P.max_block) : 0;
     Layout L;
     P.o_img = L.take(sizeof(DevImage) * n);
@@ -1007,7 +1007,7 @@ int r2p_engine_set_tuning(r2p_engine* e, int n, const r2p_tuning* classes)
     for (int i = 0; i < n; i++) {
         const r2p_tuning& c = classes[i];
         if (c.block_size < 1024 || c.block_size > kBlock64 || (c.block_size & 15) || c.band_rows < 0 ||
-            (c.hash_bits != 10 && c.hash_bits != 11) || (i > 0 && c.max_raw_bytes <= classes[i - 1].max_raw_bytes))
+            (c.hash_bits != 9 && c.hash_bits != 10) || (i > 0 && c.max_raw_bytes <= classes[i - 1].max_raw_bytes))
             return set_err(R2P_EINVAL, "tuning class out of range or not sorted by max_raw_bytes");
         t.push_back(c);
     }

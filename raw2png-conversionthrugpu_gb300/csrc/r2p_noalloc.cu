@@ -75,7 +75,7 @@ __global__ void k_noalloc_plan(DevImage* d, BlockOut* bo, const uint8_t* in, uin
         z.filt = const_cast<uint8_t*>(in);
         z.level = level;
         z.block_size = bs;
-        z.hash_bits = 11;
+        z.hash_bits = 10;
         z.nblocks = nb;
         z.out_kind = 1;
         z.prefix = 2;
@@ -180,7 +180,7 @@ extern "C" int r2p_zlib_compress_noalloc(const void* d_in, size_t len, int level
     if (e != cudaSuccess) return na_fail(e, "k_noalloc_plan");
     const int grid = (int)std::min<size_t>(nb, (size_t)nd.nsm * 8);
     if (level == 0) e = launch_stored(dimg, dblk, (int)nb, bs, xpow, grid, s);
-    else e = launch_lz77(dimg, dblk, (int)nb, bs, slots, slot, xpow, grid, 11, s);
+    else e = launch_lz77(dimg, dblk, (int)nb, bs, slots, slot, xpow, grid, 10, s);
     if (e != cudaSuccess) return na_fail(e, "DEFLATE blocks");
     e = launch_finalize(dimg, 1, dblk, xpow, s);
     if (e != cudaSuccess) return na_fail(e, "k_finalize");

@@ -57,8 +57,8 @@ def test_batch_direct_and_graph(engine, O, r2p, W):
 
 def test_tuning_table_changes_blocks_not_pixels(O, r2p, W):
     eng = r2p.Engine(0)
-    eng.set_tuning([(300000, 4096, 8, 10), (2 ** 40, 32752, 0, 11)])
-    assert eng.get_tuning()[0] == (300000, 4096, 8, 10)
+    eng.set_tuning([(300000, 4096, 8, 9), (2 ** 40, 32752, 0, 10)])
+    assert eng.get_tuning()[0] == (300000, 4096, 8, 9)
     imgs, raws, bufs, outs, caps, lens = make_batch_inputs(r2p, W, SPECS)
     b = eng.batch(imgs, [x.ptr for x in bufs], [o.ptr for o in outs], caps, lens.ptr)
     b.launch_graph()
@@ -67,7 +67,7 @@ def test_tuning_table_changes_blocks_not_pixels(O, r2p, W):
         decode_and_check(O, r2p, imgs[i], raws[i], pngs[i])
     b.close()
     with pytest.raises(r2p.R2PError):
-        eng.set_tuning([(100, 4096, 0, 12)])
+        eng.set_tuning([(100, 4096, 0, 11)])
     eng.set_tuning([])
     assert eng.get_tuning()[0][1] == r2p.BLOCK64
     eng.close()
@@ -77,7 +77,7 @@ def test_mixed_tuning_classes_same_as_alone(O, r2p, W):
     """Images of different size classes (different block sizes and LZ77 table
     sizes) in one batch give the same bytes as each image encoded alone."""
     eng = r2p.Engine(0)
-    eng.set_tuning([(200000, 32752, 0, 10), (2 ** 40, 65520, 0, 11)])
+    eng.set_tuning([(200000, 32752, 0, 9), (2 ** 40, 65520, 0, 10)])
     specs = [(256, 256, 40.0, 400.0), (700, 600, -300.0, 1500.0), (300, 200, 100.0, 90.0), (640, 640, 0.0, 800.0)]
     imgs, raws, bufs, outs, caps, lens = make_batch_inputs(r2p, W, specs)
     b = eng.batch(imgs, [x.ptr for x in bufs], [o.ptr for o in outs], caps, lens.ptr)
