@@ -312,9 +312,12 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
     P.slots_total = e->nsm * cps;
     uint64_t lut_total = 0, filt_total = 0;
     bool any10 = false;
-    // Row bands of the filter stage.  Tuned band heights suit batches of many
-    // images; when they would leave resident CTA slots idle (a lone image, a
-    // small batch) every image is split evenly instead.
+    // Row bands of the filter stage.  Batches use the tuned band height of
+    // each image's size class (0 = about kAutoBandBytes of filtered output
+    // per band: a property of the image, the same alone or in any batch).
+    // When that would leave resident CTA slots idle (a lone image, a small
+    // batch) every image is split evenly over the slots instead.
+    constexpr uint64_t kAutoBandBytes = 64 * 1024;
     auto plan_bands = [&](bool tuned) {
         P.items.clear();
         if (P.smem <= 0) return;
@@ -325,6 +328,8 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
             uint64_t band_rows;
             if (tuned && plans[i].band_rows > 0) {
                 band_rows = ((uint64_t)plans[i].band_rows + T - 1) / T * T;    // tuned, whole tiles
+            } else if (tuned) {
+                band_rows = std::max<uint64_t>(1, (kAutoBandBytes + d.rb) / ((uint64_t)d.rb + 1));
             } else {
                 // about one band per resident CTA (a lone image), split evenly;
                 // a band's last tile may be partial
