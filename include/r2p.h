@@ -214,6 +214,33 @@ int r2p_deflate_raw_device(r2p_engine* eng, const void* d_in, size_t len, int le
 int r2p_zlib_compress_noalloc(const void* d_in, size_t len, int level, int block_size,
                               void* d_out, size_t out_cap, uint64_t* d_out_len, void* stream);
 
+/* ---- BMP export -------------------------------------------------------- */
+/* Uncompressed BMP file of an image, written on the device: replaces
+ * run_bmp_from_source + BmpWriter (src/pipeline.cpp:1944-2004,
+ * src/bmp_writer.cpp:36-131) behind encode_{dicom,tiff,raw,source}_to_bmp
+ * (include/pipeline.h:97-122).  Layout: 14-byte file header, 40-byte info
+ * header with negative height (rows top to bottom), a 256-entry gray palette
+ * for one channel, rows padded with zeros to 4 bytes; one channel gives 8-bit
+ * gray, three or four give 24-bit BGR (alpha dropped).  Pixel sources:
+ *   DICOM16, 16-bit gray   the reference BMP path's own FP32 window formula
+ *                          (src/pipeline.cpp:1894-1932; it divides by the
+ *                          window range where the BATCH8 table multiplies)
+ *   BATCH8                 the folder batch's 16->8-bit rule (Q15 or table),
+ *                          as its BMP output does (src/batch_processor.cpp:389-422)
+ *   NONE, 16-bit           the first byte of each sample (the high byte of the
+ *                          big-endian samples the TIFF/RAW loaders produce)
+ *   SWAP16                 the high byte of little-endian samples
+ *   DICOM16, 16-bit colour the first byte of each sample, as the reference
+ *   8-bit samples          as they are
+ * 8-bit RGBA is refused (R2P_EINVAL).  level, strip_height and block_size are
+ * ignored.  r2p_bmp_bound gives the exact file size (0 = not exportable). */
+size_t r2p_bmp_bound(const r2p_image* img);
+int r2p_encode_bmp(r2p_engine* eng, const r2p_image* img, const void* h_pixels, void* h_bmp,
+                   size_t bmp_cap, size_t* bmp_len);
+/* Device buffers; d_bmp must be 4-byte aligned and hold r2p_bmp_bound bytes. */
+int r2p_encode_bmp_device(r2p_engine* eng, const r2p_image* img, const void* d_pixels, void* d_bmp,
+                          size_t bmp_cap, void* stream);
+
 /* ---- serving: continuous batching ------------------------------------- */
 /* A server owns a device (an engine), a pooled device arena of hbm_budget
  * bytes and a pinned host pool.  Requests are admitted against the budget;

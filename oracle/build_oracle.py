@@ -7,6 +7,7 @@ Outputs:
   oracle/_ref/...      -- built only where the reference tree is present, from
                           the reference's own sources, left where they lie:
      libref_window.so   src/batch_processor.cpp via ref_window_harness.cpp
+     ref_bmp_runner     src/pipeline.cpp + src/bmp_writer.cpp via ref_bmp_harness.cpp
      libref_cpu.so      src/parallel_deflate.cpp + src/png_writer.cpp via
                         ref_cpu_harness.cpp
      gpu_filter_ref_fastmath.cubin / gpu_filter_ref_ieee.cubin
@@ -80,6 +81,13 @@ def build_ref(verbose=False):
                                       os.path.join(REF, "src", "parallel_deflate.cpp"),
                                       os.path.join(REF, "src", "png_writer.cpp"),
                                       "-o", cpu, "-lz", "-lpthread"], verbose)
+    # the reference's BMP export: src/pipeline.cpp + src/bmp_writer.cpp run by
+    # a small executable (unresolved GPU/decoder symbols are never reached)
+    bmp = os.path.join(REF_DIR, "ref_bmp_runner")
+    if not _newer(bmp, [os.path.join(HERE, "ref_bmp_harness.cpp")]):
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-w"] + inc +
+             [os.path.join(HERE, "ref_bmp_harness.cpp"), "-o", bmp,
+              "-Wl,--unresolved-symbols=ignore-all", "-lpthread"], verbose)
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     cu = os.path.join(REF, "src", "gpu_filter.cu")
     for tag, extra in (("fastmath", ["--use_fast_math"]),

@@ -286,6 +286,62 @@ int orc_window8(const uint8_t* src_le, size_t n, const orc_params* p, uint8_t* d
 }
 
 /* ------------------------------------------------------------------------
+ * BMP export windowing: dicom16_row_to_gray8 (src/pipeline.cpp:1894-1932),
+ * 16-bit LE grayscale DICOM -> 8-bit gray, with the normalisation constants
+ * run_bmp_from_source passes it (:1953-1963).  Differs from the batch table
+ * (orc_build_lut) only in dividing by (hi - lo) instead of multiplying by
+ * its reciprocal.  Requires 0 <= high_bit - bits_stored + 1.
+ * ---------------------------------------------------------------------- */
+void orc_bmp_gray8(const uint8_t* src_le, size_t n, const orc_params* p, uint8_t* dst8)
+{
+    float norm_scale = 1.f, norm_offset = 0.f;
+    if (!p->apply_window) {                                       /* :1953-1963 */
+        if (p->pixel_rep == 1) {
+            const float half  = (float)(1u << (p->bits_stored - 1));
+            const float range = (float)(1u << p->bits_stored);
+            norm_scale  = 1.f / range;
+            norm_offset = half / range;
+        } else {
+            norm_scale = 1.f / (float)((1u << p->bits_stored) - 1u);
+        }
+    }
+    const int shift = p->high_bit - p->bits_stored + 1;          /* :1899-1900 */
+    const int mask  = (p->bits_stored < 32) ? ((1 << p->bits_stored) - 1) : -1;
+    for (size_t i = 0; i < n; i++) {
+        uint16_t raw = (uint16_t)((unsigned)src_le[i * 2] | ((unsigned)src_le[i * 2 + 1] << 8));
+        raw = (uint16_t)((raw >> shift) & mask);
+        float val;                                                /* :1906-1916 */
+        if (p->pixel_rep == 1 && p->bits_stored < 16) {
+            const int sign_bit = 1 << (p->bits_stored - 1);
+            int32_t s = (int32_t)(uint32_t)raw;
+            if (s & sign_bit) s |= ~((int32_t)mask);
+            val = (float)s;
+        } else if (p->pixel_rep == 1) {
+            val = (float)(int16_t)raw;
+        } else {
+            val = (float)raw;
+        }
+        if (p->apply_rescale) {                                   /* :1918-1919 */
+            float m = val * p->rescale_slope;
+            val = m + p->rescale_intercept;
+        }
+        float norm;                                               /* :1921-1928 */
+        if (p->apply_window) {
+            const float h  = p->window_width * 0.5f;
+            const float lo = p->window_center - h;
+            const float hi = p->window_center + h;
+            norm = (hi > lo) ? (val - lo) / (hi - lo) : 0.f;
+        } else {
+            float m = val * norm_scale;
+            norm = m + norm_offset;
+        }
+        float s255 = norm * 255.f;                                /* :1930-1931 */
+        const int v = (int)(s255 + 0.5f);
+        dst8[i] = (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+    }
+}
+
+/* ------------------------------------------------------------------------
  * Adaptive PNG filter: src/gpu_filter.cu:183-309 (filter_select_kernel).
  *   img   : rows x rb windowed bytes (PNG byte order)
  *   prior : rb bytes seen as the row above row 0 (NULL = zeros)

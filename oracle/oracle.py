@@ -79,6 +79,7 @@ def lib():
         L.orc_q15_coeffs.argtypes = [P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
         L.orc_q15_coeffs.restype = ctypes.c_int
         L.orc_build_lut.argtypes = [_u8p, P, ctypes.c_int]
+        L.orc_bmp_gray8.argtypes = [_u8p, ctypes.c_size_t, P, _u8p]
         L.orc_filter_rows.argtypes = [_u8p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u8p]
         L.orc_unfilter.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u8p]
         L.orc_unfilter.restype = ctypes.c_int
@@ -128,6 +129,51 @@ def build_lut(p):
     lut = np.empty(n, np.uint8)
     lib().orc_build_lut(_ptr(lut), ctypes.byref(p), n)
     return lut
+
+
+# ---------------------------------------------------------------------- BMP
+def bmp_gray8(raw_le, p):
+    """BMP export window (src/pipeline.cpp:1894-1932): 16-bit LE -> 8-bit."""
+    raw_le = np.ascontiguousarray(raw_le, dtype=np.uint8).reshape(-1)
+    out = np.empty(raw_le.size // 2, np.uint8)
+    lib().orc_bmp_gray8(_ptr(raw_le), out.size, ctypes.byref(p), _ptr(out))
+    return out
+
+
+def bmp_file(raw, width, height, channels, bytes_per_sample, mode, p=None):
+    """Whole BMP file of an image as the reference's BMP export writes it
+    (run_bmp_from_source src/pipeline.cpp:1944-2004; BmpWriter
+    src/bmp_writer.cpp:36-131).  mode: 'dicom' (a DICOM source), 'batch8'
+    (the folder batch's 16->8 rule, src/batch_processor.cpp:389-422), 'be'
+    (16-bit big-endian samples, e.g. TIFF/RAW) or 'le' (16-bit little-endian
+    samples: the high byte is second)."""
+    raw = np.ascontiguousarray(raw, dtype=np.uint8).reshape(-1)
+    oc = 1 if channels == 1 else 3
+    if mode == "batch8":
+        px, _ = window8(raw, p)
+        px = px.reshape(height, width, 1)
+    elif mode == "dicom" and bytes_per_sample == 2 and channels == 1:
+        px = bmp_gray8(raw, p).reshape(height, width, 1)
+    elif bytes_per_sample == 2:
+        s = raw.reshape(height, width, channels, 2)[..., 1 if mode == "le" else 0]
+        px = s[..., :oc]
+    else:
+        px = raw.reshape(height, width, channels)[..., :oc]
+    if oc == 3:
+        px = px[..., ::-1]                                   # RGB -> BGR
+    stride = (width * oc + 3) & ~3
+    rows = np.zeros((height, stride), np.uint8)
+    rows[:, :width * oc] = px.reshape(height, width * oc)
+    pix_off = 54 + (1024 if oc == 1 else 0)
+    size = pix_off + stride * height
+    head = struct.pack("<2sIIIIiiHHIIiiII", b"BM", size, 0, pix_off, 40, width, -height, 1,
+                       8 if oc == 1 else 24, 0, 0, 0, 0, 256 if oc == 1 else 0, 0)
+    pal = b""
+    if oc == 1:
+        pal = np.repeat(np.arange(256, dtype=np.uint8), 4).reshape(256, 4)
+        pal[:, 3] = 0
+        pal = pal.tobytes()
+    return head + pal + rows.tobytes()
 
 
 # ------------------------------------------------------------------- filter
@@ -254,6 +300,33 @@ def ref_window_lib():
         L.ref_build_dicom16_lut.argtypes = [_u8p, P, ctypes.c_int]
         _ref_win = L
     return _ref_win
+
+
+def ref_bmp_runner():
+    """Path of oracle/_ref/ref_bmp_runner (the reference's BMP export), or None."""
+    path = os.path.join(HERE, "_ref", "ref_bmp_runner")
+    return path if os.path.exists(path) else None
+
+
+def ref_bmp_file(raw, width, height, channels, bits_per_sample, p=None, workdir=None):
+    """BMP bytes the reference's own encode_source_to_bmp writes for an image
+    (p: DicomPixelParams of a DICOM source, None for TIFF/RAW)."""
+    import subprocess
+    import tempfile
+    runner = ref_bmp_runner()
+    assert runner, "reference BMP runner not built"
+    with tempfile.TemporaryDirectory(dir=workdir) as td:
+        src, dst = os.path.join(td, "in.raw"), os.path.join(td, "out.bmp")
+        np.ascontiguousarray(raw, dtype=np.uint8).tofile(src)
+        q = p if p is not None else make_params()
+        args = [runner, src, dst, str(width), str(height), str(channels), str(bits_per_sample),
+                "1" if p is not None else "0", str(q.bits_allocated), str(q.bits_stored), str(q.high_bit),
+                str(q.pixel_rep), str(q.apply_rescale), float(q.rescale_slope).hex(),
+                float(q.rescale_intercept).hex(), str(q.apply_window), float(q.window_center).hex(),
+                float(q.window_width).hex()]
+        subprocess.run(args, check=True)
+        with open(dst, "rb") as f:
+            return f.read()
 
 
 def ref_window8(raw_le, p):

@@ -155,6 +155,9 @@ SIGNATURES = {
                                                ctypes.POINTER(_vp), ctypes.POINTER(_sz), _vp, _vp]),
     "r2p_window_filter_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp]),
     "r2p_window_filter_device_ex": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp, _vp]),
+    "r2p_bmp_bound": (_sz, [ctypes.POINTER(Image)]),
+    "r2p_encode_bmp": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _sz, ctypes.POINTER(_sz)]),
+    "r2p_encode_bmp_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _sz, _vp]),
     "r2p_zlib_compress_device": (ctypes.c_int, [_vp, _vp, _sz, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _vp]),
     "r2p_zlib_bound": (_sz, [_sz, ctypes.c_int, ctypes.c_int]),
     "r2p_deflate_raw_device": (ctypes.c_int, [_vp, _vp, _sz, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp,
@@ -228,6 +231,10 @@ def check(status):
 
 def png_bound(img):
     return lib().r2p_png_bound(ctypes.byref(img))
+
+
+def bmp_bound(img):
+    return lib().r2p_bmp_bound(ctypes.byref(img))
 
 
 def zlib_bound(n, level, block_size=0):
@@ -394,6 +401,22 @@ class Engine:
         n = _sz()
         check(lib().r2p_encode_png(self.h, ctypes.byref(img), px.ctypes.data, out.ctypes.data, cap, ctypes.byref(n)))
         return out[:n.value].tobytes()
+
+    def encode_bmp(self, img, pixels):
+        """Host pixels -> BMP file bytes (blocking; r2p_encode_bmp)."""
+        px = np.ascontiguousarray(pixels).view(np.uint8).reshape(-1)
+        assert px.nbytes == img.raw_bytes, (px.nbytes, img.raw_bytes)
+        cap = bmp_bound(img)
+        if cap == 0:
+            check(EINVAL)
+        out = np.empty(cap, np.uint8)
+        n = _sz()
+        check(lib().r2p_encode_bmp(self.h, ctypes.byref(img), px.ctypes.data, out.ctypes.data, cap, ctypes.byref(n)))
+        return out[:n.value].tobytes()
+
+    def encode_bmp_device(self, img, d_pixels, d_bmp, cap, stream=None):
+        """Device pixels -> BMP file in device memory (r2p_encode_bmp_device)."""
+        check(lib().r2p_encode_bmp_device(self.h, ctypes.byref(img), d_pixels, d_bmp, cap, _sp(stream)))
 
     def encode_png_many(self, imgs, inputs, outputs=None):
         """Host images -> PNGs with up to MANY_SLOTS images in flight

@@ -59,7 +59,8 @@ HOST = os.path.join(HERE, "host")
 HOST_LIB = os.path.join(HERE, "libr2p_host.so")
 CLI = os.path.join(HERE, "gpu_png_encoder")
 HOST_SOURCES = ["gpu_filter.cpp", "compression_backend.cpp", "parallel_deflate.cpp", "png_writer.cpp",
-                "file_type.cpp", "dicom_loader.cpp", "image_loader.cpp", "pipeline.cpp", "batch_processor.cpp"]
+                "file_type.cpp", "dicom_loader.cpp", "image_loader.cpp", "bmp_writer.cpp", "pipeline.cpp",
+                "batch_processor.cpp"]
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter", "-ffp-contract=off",
              "-I" + os.path.join(HOST, "include"), "-I" + INCLUDE]
 

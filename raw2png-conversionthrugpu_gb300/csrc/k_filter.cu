@@ -20,6 +20,8 @@
 // the oracle's -ffp-contract=off restatement bit for bit.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "r2p_common.h"
 #include "r2p_device.h"
 #include "r2p_kernels.h"
@@ -87,8 +89,12 @@ __device__ __forceinline__ uint32_t win_index(uint32_t raw, int shift, uint32_t 
     return (raw >> shift) & mask;
 }
 
-// FP32 table entry of build_dicom16_lut (src/batch_processor.cpp:100-147).
-__device__ uint8_t lut8_eval(int i, int lut_size, const r2p_dicom_params& p)
+// FP32 table entry of build_dicom16_lut (src/batch_processor.cpp:100-147);
+// with divide, the per-pixel formula of the BMP export, dicom16_row_to_gray8
+// (src/pipeline.cpp:1894-1932, normalisation constants :1953-1963): the same
+// steps except that the window divides by (hi - lo) where the table
+// multiplies by its reciprocal.
+__device__ uint8_t lut8_eval(int i, int lut_size, const r2p_dicom_params& p, bool divide = false)
 {
     const int mask = lut_size - 1;
     float norm_scale = 1.f, norm_offset = 0.f;
@@ -120,8 +126,14 @@ __device__ uint8_t lut8_eval(int i, int lut_size, const r2p_dicom_params& p)
         val = (float)(unsigned)i;
     }
     if (p.apply_rescale) val = __fadd_rn(__fmul_rn(val, p.rescale_slope), p.rescale_intercept);
-    const float norm = p.apply_window ? __fmul_rn(__fsub_rn(val, lo), inv_range)
-                                      : __fadd_rn(__fmul_rn(val, norm_scale), norm_offset);
+    float norm;
+    if (p.apply_window && divide) {
+        const float hi = __fadd_rn(p.window_center, __fmul_rn(p.window_width, 0.5f));
+        norm = (hi > lo) ? __fdiv_rn(__fsub_rn(val, lo), __fsub_rn(hi, lo)) : 0.f;
+    } else {
+        norm = p.apply_window ? __fmul_rn(__fsub_rn(val, lo), inv_range)
+                              : __fadd_rn(__fmul_rn(val, norm_scale), norm_offset);
+    }
     const int v = __float2int_rz(__fadd_rn(__fmul_rn(norm, 255.f), 0.5f));
     return (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
 }
@@ -196,6 +208,13 @@ __global__ void k_prepare_window(DevImage* imgs, int n)
             d.lut_entries = entries;
             d.lut_esize = d.ob;
             mode = (entries * d.ob <= kMaxSmemLut) ? W_A2_LUT : W_A2_DIRECT;
+        } else if (d.req_mode == kReqBmp8) {
+            const int entries = 1 << p.bits_stored;
+            d.lut_entries = entries;
+            d.lut_esize = 1;
+            d.lut_shift = p.high_bit - p.bits_stored + 1;
+            d.lut_mask = (uint32_t)(entries - 1);
+            mode = W_LUT8;
         } else if (d.req_mode == R2P_WINDOW_BATCH8) {
             int32_t A, B;
             if (q15_coeffs(p, A, B)) {
@@ -229,7 +248,8 @@ __global__ void k_prepare_window(DevImage* imgs, int n)
         }
     } else if (mode == W_LUT8) {
         const int n_e = d.lut_entries;
-        for (int i = threadIdx.x; i < n_e; i += blockDim.x) d.lut[i] = lut8_eval(i, n_e, d.dp);
+        const bool divide = d.req_mode == kReqBmp8;
+        for (int i = threadIdx.x; i < n_e; i += blockDim.x) d.lut[i] = lut8_eval(i, n_e, d.dp, divide);
     }
 }
 
@@ -821,6 +841,94 @@ k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items,
     }
 }
 
+// ---------------------------------------------------------------------------
+// BMP export
+// ---------------------------------------------------------------------------
+// File layout of the reference's BmpWriter (src/bmp_writer.cpp:36-96 header
+// and palette, :98-131 rows): BITMAPFILEHEADER (14) + BITMAPINFOHEADER (40,
+// negative height: rows top to bottom) + a 256-entry gray palette (8-bit
+// output only) + rows of width * oc bytes (BGR for colour) zero-padded to a
+// multiple of 4.  Pixel sources follow run_bmp_from_source
+// (src/pipeline.cpp:1965-2001).
+
+// Byte fb (< 54) of the two headers, little-endian fields.
+__device__ uint32_t bmp_header_byte(const DevImage& d, uint32_t fb)
+{
+    if (fb < 2) return fb == 0 ? 0x42u : 0x4Du;            // "BM"
+    uint32_t field;
+    uint32_t at;
+    if (fb < 6) { field = d.bmp_size; at = 2; }
+    else if (fb < 10) return 0u;                         // reserved
+    else if (fb < 14) { field = d.bmp_pix_off; at = 10; }
+    else if (fb < 18) { field = 40u; at = 14; }          // biSize
+    else if (fb < 22) { field = d.width; at = 18; }
+    else if (fb < 26) { field = (uint32_t)(-(int32_t)d.height); at = 22; }
+    else if (fb < 28) { field = 1u; at = 26; }           // biPlanes
+    else if (fb < 30) { field = d.bmp_oc == 1 ? 8u : 24u; at = 28; }
+    else if (fb >= 46 && fb < 50) { field = d.bmp_oc == 1 ? 256u : 0u; at = 46; }   // biClrUsed
+    else return 0u;
+    return (field >> (8 * (fb - at))) & 0xFFu;
+}
+
+// One output pixel byte: row r, byte col (< width * oc) of the unpadded row.
+__device__ __forceinline__ uint32_t bmp_pixel_byte(const DevImage& d, const WinCtx& w, uint32_t r, uint32_t col)
+{
+    const uint32_t oc = (uint32_t)d.bmp_oc;
+    const uint32_t x = oc == 1 ? col : col / 3u;
+    const uint32_t c = col - x * oc;
+    const uint32_t si = x * (uint32_t)d.channels + (oc == 3 ? 2u - c : 0u);   // RGB -> BGR
+    const uint8_t* row = d.raw + (size_t)r * (size_t)d.in_pitch;
+    if (d.bmp_kind == BMP_BYTE) return __ldg(row + si);
+    if (d.bmp_kind == BMP_TAKE) return __ldg(row + 2 * si + d.bmp_off);
+    const uint32_t raw = (uint32_t)__ldg(row + 2 * si) | ((uint32_t)__ldg(row + 2 * si + 1) << 8);
+    return d.mode == W_Q15 ? win_sample<K_Q15>(w, raw) : win_sample<K_LUT8>(w, raw);
+}
+
+// Whole BMP files, one 4-byte file word per thread (image blockIdx.y); the
+// output buffer is 4-byte aligned.
+__global__ void __launch_bounds__(256) k_bmp_file(const DevImage* __restrict__ imgs)
+{
+    const DevImage& d = imgs[blockIdx.y];
+    WinCtx w;
+    w.mode = d.mode; w.ib = d.ib; w.ob = 1; w.shift = d.lut_shift; w.mask = d.lut_mask;
+    w.qa = d.qa; w.qb = d.qb; w.dp = d.dp;
+    w.lut = d.lut;
+    const uint32_t nwords = (d.bmp_size + 3u) >> 2;
+    const uint32_t rowbytes = d.width * (uint32_t)d.bmp_oc, stride = (uint32_t)d.bmp_stride;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nwords; k += gridDim.x * blockDim.x) {
+        const uint32_t fb0 = 4u * k;
+        uint32_t word = 0;
+        // row and column of the word's first pixel byte, stepped per byte
+        uint32_t r = 0, col = 0;
+        if (fb0 + 3u >= d.bmp_pix_off) {
+            const uint32_t pb = fb0 > d.bmp_pix_off ? fb0 - d.bmp_pix_off : 0u;
+            r = pb / stride;
+            col = pb - r * stride;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t fb = fb0 + (uint32_t)j;
+            uint32_t v = 0;
+            if (fb < 54u) {
+                v = bmp_header_byte(d, fb);
+            } else if (fb < d.bmp_pix_off) {
+                const uint32_t q = fb - 54u;                    // gray palette: B = G = R = i, 0
+                v = (q & 3u) == 3u ? 0u : (q >> 2);
+            } else if (fb < d.bmp_size) {
+                if (col < rowbytes) v = bmp_pixel_byte(d, w, r, col);
+                if (++col == stride) { col = 0; r++; }
+            }
+            word |= v << (8 * j);
+        }
+        uint8_t* out = d.png + fb0;
+        if (fb0 + 4u <= d.bmp_size) {
+            *reinterpret_cast<uint32_t*>(out) = word;
+        } else {
+            for (uint32_t j = 0; fb0 + j < d.bmp_size; j++) out[j] = (uint8_t)(word >> (8 * j));
+        }
+    }
+}
+
 }  // namespace r2p
 
 namespace r2p {
@@ -875,6 +983,15 @@ int filter_ctas_per_sm(int smem)
 cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s)
 {
     k_prepare_window<<<n, 256, 0, s>>>(imgs, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bmp(DevImage* imgs, int n, uint32_t max_words, int nsm, cudaStream_t s)
+{
+    const uint32_t want = (max_words + 255u) / 256u;
+    const dim3 grid((unsigned)std::max<uint32_t>(1u, std::min<uint32_t>(want, (uint32_t)nsm * 8u)), (unsigned)n);
+    k_bmp_file<<<grid, 256, 0, s>>>(imgs);
     note_launch();
     return cudaGetLastError();
 }

@@ -18,6 +18,17 @@ enum WinMode : int {
     W_LUT8 = 5,      // 16-bit LE in, 8-bit out, FP32-built table
 };
 
+// Internal window request of the BMP export: the 16-bit DICOM to 8-bit gray
+// formula of the reference's BMP path, resolved to a W_LUT8 table.
+constexpr int kReqBmp8 = 0x100;
+
+// Source of a BMP output byte.
+enum BmpKind : int {
+    BMP_BYTE = 0,     // 8-bit sample as is
+    BMP_TAKE = 1,     // one byte of a 16-bit sample (bmp_off: 0 or 1)
+    BMP_WINDOW = 2,   // 16-bit sample through the resolved 8-bit window (W_Q15 / W_LUT8)
+};
+
 // Largest table kept in shared memory by the filter kernel (bytes).
 constexpr int kMaxSmemLut = 32768;
 
@@ -57,6 +68,10 @@ struct DevImage {
     uint64_t* png_len;              // device word receiving the PNG size (or error bit)
     uint32_t idat_crc_partial;      // scratch
     int32_t status;                 // device-side error code (0 = ok)
+    // BMP export (png = the file buffer)
+    int32_t bmp_kind, bmp_off;      // BmpKind, byte of a 16-bit sample taken by BMP_TAKE
+    int32_t bmp_oc, bmp_stride;     // output channels (1 or 3), padded row bytes
+    uint32_t bmp_pix_off, bmp_size; // pixel array offset, file bytes
 };
 
 // A band of consecutive rows of one image, filtered by one CTA.

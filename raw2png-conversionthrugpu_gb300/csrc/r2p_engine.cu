@@ -189,6 +189,84 @@ static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip,
     return R2P_OK;
 }
 
+// BMP export plan.  The window request maps onto the pixel sources of the
+// reference's BMP path (src/pipeline.cpp:1965-2001): a 16-bit grayscale DICOM
+// frame through its own FP32 formula (as a table), BATCH8 through the folder
+// batch's 16->8-bit rule (src/batch_processor.cpp:389-422), other 16-bit
+// samples by one byte (the first: big-endian data as the loaders leave it,
+// and the reference's choice for 16-bit colour DICOM too), 8-bit samples as
+// they are.
+static int plan_bmp(const r2p_image& im, ImgPlan& ip)
+{
+    if (im.width < 1 || im.height < 1) return set_err(R2P_EINVAL, "width and height must be >= 1");
+    if (im.channels != 1 && im.channels != 3 && im.channels != 4)
+        return set_err(R2P_EINVAL, "channels must be 1, 3 or 4");
+    if (im.bytes_per_sample != 1 && im.bytes_per_sample != 2)
+        return set_err(R2P_EINVAL, "bytes_per_sample must be 1 or 2");
+    if (im.bytes_per_sample == 1 && im.channels == 4)
+        return set_err(R2P_EINVAL, "8-bit RGBA has no BMP form here (the reference reads such rows as RGB triplets)");
+    const r2p_dicom_params& p = im.dicom;
+    DevImage& d = ip.di;
+    memset(&d, 0, sizeof(d));
+    d.width = im.width;
+    d.height = im.height;
+    d.channels = im.channels;
+    d.ib = im.bytes_per_sample;
+    d.ob = 1;
+    d.in_pitch = (int32_t)((uint64_t)im.width * im.channels * im.bytes_per_sample);
+    d.req_mode = R2P_WINDOW_NONE;
+    d.dp = p;
+    d.block_size = kBlock64;
+    int entries = 0;
+    d.bmp_kind = im.bytes_per_sample == 2 ? BMP_TAKE : BMP_BYTE;
+    switch (im.window_mode) {
+        case R2P_WINDOW_NONE:
+            break;
+        case R2P_WINDOW_SWAP16:
+            if (im.bytes_per_sample != 2) return set_err(R2P_EINVAL, "SWAP16 needs 16-bit samples");
+            d.bmp_off = 1;                        // little-endian samples: the high byte is second
+            break;
+        case R2P_WINDOW_DICOM16:
+            if (p.bits_allocated != 8 * im.bytes_per_sample)
+                return set_err(R2P_EINVAL, "DICOM16: bits_allocated must match bytes_per_sample");
+            if (p.bits_stored < 1 || p.bits_stored > p.bits_allocated)
+                return set_err(R2P_EINVAL, "DICOM16: bits_stored out of range");
+            if (im.bytes_per_sample == 2 && im.channels == 1) {
+                if (p.high_bit - p.bits_stored + 1 < 0 || p.high_bit > 15)
+                    return set_err(R2P_EINVAL, "DICOM16: high_bit out of range");
+                d.req_mode = kReqBmp8;
+                d.bmp_kind = BMP_WINDOW;
+                entries = 1 << p.bits_stored;
+            }
+            break;
+        case R2P_WINDOW_BATCH8:
+            if (im.bytes_per_sample != 2 || im.channels != 1)
+                return set_err(R2P_EINVAL, "BATCH8 needs 16-bit grayscale samples");
+            if (p.bits_stored < 1 || p.bits_stored > 16 || p.high_bit - p.bits_stored + 1 < 0 || p.high_bit > 15)
+                return set_err(R2P_EINVAL, "BATCH8: bits_stored/high_bit out of range");
+            d.req_mode = R2P_WINDOW_BATCH8;
+            d.bmp_kind = BMP_WINDOW;
+            entries = 1 << p.bits_stored;
+            break;
+        default:
+            return set_err(R2P_EINVAL, "unknown window_mode");
+    }
+    d.bmp_oc = im.channels == 1 ? 1 : 3;
+    const uint64_t stride = ((uint64_t)im.width * d.bmp_oc + 3) & ~3ull;
+    const uint64_t pix_off = 54 + (d.bmp_oc == 1 ? 1024 : 0);
+    const uint64_t size = pix_off + stride * im.height;
+    if (size >= (1ull << 31)) return set_err(R2P_EINVAL, "BMP file would exceed 2 GiB");
+    d.bmp_stride = (int32_t)stride;
+    d.bmp_pix_off = (uint32_t)pix_off;
+    d.bmp_size = (uint32_t)size;
+    ip.raw_bytes = (uint64_t)d.in_pitch * im.height;
+    ip.lut_cap = align_up((uint64_t)entries + 16, 256);
+    ip.png_bound = size;
+    ip.smem = 0;
+    ip.lreg = 0;
+    return R2P_OK;
+}
+
 }  // namespace r2p
 
 using namespace r2p;
@@ -253,7 +331,7 @@ struct CallBuffers {
     std::vector<uint64_t*> out_len;
 };
 
-enum Stages { ST_FILTER = 1, ST_DEFLATE = 2, ST_ALL = 3 };
+enum Stages { ST_FILTER = 1, ST_DEFLATE = 2, ST_ALL = 3, ST_BMP = 4 };
 
 static int ensure_arena(r2p_engine* e, size_t need)
 {
@@ -300,6 +378,7 @@ struct Prepared {
     size_t total = 0;
     int hash_bits = 10;
     int stage_slot = 0;
+    uint32_t bmp_words = 0;    // 4-byte words of the largest BMP file
 };
 
 // Work list and memory layout of one call (or one batch) over n images.
@@ -362,6 +441,7 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
         if (d.level > 0 && d.hash_bits == 10) any10 = true;
         lut_total += plans[i].lut_cap;
         if (!cb.filt[i]) filt_total += align_up(d.filt_bytes + 64, 256);
+        P.bmp_words = std::max(P.bmp_words, (d.bmp_size + 3u) / 4u);
     }
     // one hash-table size per launch: the one most blocks were tuned for
     P.hash_bits = any10 ? 10 : 9;      // LZ77 tables sized for the largest; each block uses its image's
@@ -422,15 +502,16 @@ static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, in
         if (ran) *tmask |= 1u << (k - 1);
         return cudaEventRecord(tev[k], s);
     };
-    const bool filt = (stages & ST_FILTER) != 0, defl = (stages & ST_DEFLATE) != 0;
+    const bool filt = (stages & ST_FILTER) != 0, defl = (stages & ST_DEFLATE) != 0, bmp = (stages & ST_BMP) != 0;
     R2P_CU(mark(0, false), "event");
-    if (filt) R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
-    R2P_CU(mark(1, filt), "event");
+    if (filt || bmp) R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
+    R2P_CU(mark(1, filt || bmp), "event");
     if (filt) {
         const int grid = (int)std::min<size_t>(P.items.size(), (size_t)P.slots_total);
         R2P_CU(launch_window_filter(dimg, ditems, (int)P.items.size(), grid, P.smem, s), "k_window_filter");
     }
-    R2P_CU(mark(2, filt), "event");
+    if (bmp) R2P_CU(launch_bmp(dimg, n, P.bmp_words, e->nsm, s), "k_bmp_file");   // timed in the filter's slot
+    R2P_CU(mark(2, filt || bmp), "event");
     const int bgrid = (int)std::min<uint64_t>(P.nblk, (uint64_t)e->nsm * 8);
     if (defl && P.any_stored)
         R2P_CU(launch_stored(dimg, dblocks, (int)P.nblk, P.max_block, e->d_xpow, bgrid, s), "k_stored_blocks");
@@ -878,6 +959,75 @@ int r2p_window_filter_device_ex(r2p_engine* e, const r2p_image* img, const void*
     cb.out_cap = {0};
     cb.out_len = {nullptr};
     return run(e, plans, cb, ST_FILTER, static_cast<cudaStream_t>(stream));
+}
+
+size_t r2p_bmp_bound(const r2p_image* img)
+{
+    if (!img) return 0;
+    ImgPlan ip;
+    if (plan_bmp(*img, ip)) return 0;
+    return (size_t)ip.png_bound;
+}
+
+int r2p_encode_bmp_device(r2p_engine* e, const r2p_image* img, const void* d_pixels, void* d_bmp, size_t bmp_cap,
+                          void* stream)
+{
+    if (!e || !img || !d_pixels || !d_bmp) return set_err(R2P_EINVAL, "NULL argument");
+    if (reinterpret_cast<uintptr_t>(d_bmp) & 3) return set_err(R2P_EINVAL, "d_bmp must be 4-byte aligned");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    std::vector<ImgPlan> plans(1);
+    rc = plan_bmp(*img, plans[0]);
+    if (rc) return rc;
+    if (bmp_cap < plans[0].png_bound) return set_err(R2P_ENOSPC, "bmp_cap below r2p_bmp_bound()");
+    CallBuffers cb;
+    cb.raw = {static_cast<const uint8_t*>(d_pixels)};
+    cb.filt = {nullptr};
+    cb.prior = {nullptr};
+    cb.out = {static_cast<uint8_t*>(d_bmp)};
+    cb.out_cap = {bmp_cap};
+    cb.out_len = {nullptr};
+    return run(e, plans, cb, ST_BMP, static_cast<cudaStream_t>(stream));
+}
+
+int r2p_encode_bmp(r2p_engine* e, const r2p_image* img, const void* h_pixels, void* h_bmp, size_t bmp_cap,
+                   size_t* bmp_len)
+{
+    if (!e || !img || !h_pixels || !h_bmp || !bmp_len) return set_err(R2P_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(e->mu);
+    int rc = bind(e);
+    if (rc) return rc;
+    std::vector<ImgPlan> plans(1);
+    rc = plan_bmp(*img, plans[0]);
+    if (rc) return rc;
+    const size_t raw_bytes = (size_t)plans[0].raw_bytes;
+    const size_t size = (size_t)plans[0].png_bound;
+    *bmp_len = size;
+    if (bmp_cap < size) return set_err(R2P_ENOSPC, "bmp_cap below r2p_bmp_bound()");
+    const size_t raw_region = align_up(raw_bytes + 16, 256);
+    CallBuffers cb;
+    cb.raw = {nullptr};
+    cb.filt = {nullptr};
+    cb.prior = {nullptr};
+    cb.out = {nullptr};
+    cb.out_cap = {size};
+    cb.out_len = {nullptr};
+    cudaStream_t s = e->hstream;
+    Prepared P;
+    uint8_t* ext = nullptr;
+    rc = prepare(e, plans, cb, raw_region + align_up(size, 256), s, P, &ext);
+    if (rc) return rc;
+    uint8_t* d_raw = ext;
+    uint8_t* d_bmp = ext + raw_region;
+    cb.raw = {d_raw};
+    cb.out = {d_bmp};
+    R2P_CU(cudaMemcpyAsync(d_raw, h_pixels, raw_bytes, cudaMemcpyHostToDevice, s), "pixel upload");
+    rc = launch(e, plans, cb, P, ST_BMP, s);
+    if (rc) return rc;
+    R2P_CU(cudaMemcpyAsync(h_bmp, d_bmp, size, cudaMemcpyDeviceToHost, s), "bmp download");
+    R2P_CU(cudaStreamSynchronize(s), "sync");
+    return R2P_OK;
 }
 
 // One DEFLATE stream over device bytes: a zlib stream (out_kind 1) or raw

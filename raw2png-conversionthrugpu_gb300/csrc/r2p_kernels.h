@@ -11,6 +11,8 @@ void note_launch();
 
 // k_filter.cu
 cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s);
+// BMP files of n images (max_words: 4-byte words of the largest file).
+cudaError_t launch_bmp(DevImage* imgs, int n, uint32_t max_words, int nsm, cudaStream_t s);
 cudaError_t launch_window_filter(DevImage* imgs, const BandItem* items, int nitems, int grid,
                                  int smem, cudaStream_t s);
 int filter_smem_bytes(int rb, int in_pitch, int mode, int lut_entries, int lut_esize);

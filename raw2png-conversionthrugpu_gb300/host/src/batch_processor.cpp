@@ -9,6 +9,10 @@
 //                                     Q15 map when eligible, else FP32 table)
 //   other single-frame             -> <stem>.png at its own depth (R2P_WINDOW_DICOM16)
 //   multi-frame                    -> <stem>/slice_NNNN.png, own depth
+// With --format bmp single frames and TIFFs become <stem>.bmp, written by the
+// reader thread through r2p_encode_bmp (the same 16->8 rule for 16-bit
+// grayscale DICOM, src/batch_processor.cpp:389-434); multi-frame files stay
+// PNG slices, as in the reference (:378-384).
 #include "batch_processor.h"
 
 #include <algorithm>
@@ -76,10 +80,8 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
         return true;
     }
     std::sort(files.begin(), files.end());
-    if (cfg.format == ExportFormat::BMP) {
-        std::fprintf(stderr, "BMP export is not part of this build\n");
-        return false;
-    }
+    const bool bmp = cfg.format == ExportFormat::BMP;
+    const std::string ext = bmp ? ".bmp" : ".png";
     int workers = batch_cfg.num_workers;
     if (workers <= 0) {
         const int hw = (int)std::thread::hardware_concurrency();
@@ -94,7 +96,7 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
     r2p_server* srv = nullptr;
     if (!r2p_host::ok(r2p_server_create(cfg.device, &sc, &srv), "r2p_server_create")) return false;
     const int level = cfg.deflate_level < 0 ? 0 : cfg.deflate_level > 9 ? 9 : cfg.deflate_level;
-    std::printf("Batch: %zu file(s), %d reader(s), format=PNG\n", files.size(), workers);
+    std::printf("Batch: %zu file(s), %d reader(s), format=%s\n", files.size(), workers, bmp ? "BMP" : "PNG");
 
     const int kMaxOutstanding = 256;            // frames submitted but not yet written
     std::vector<FileJob> jobs(files.size());
@@ -134,6 +136,21 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
         fj.out = out;
         job.frames.push_back(fj);
         return true;
+    };
+
+    // a BMP of one loaded DICOM frame, written by this (reader) thread
+    auto write_frame_bmp = [&](DicomSource& src, int frame, int mode, const std::string& out) -> bool {
+        if (!src.load_frame(frame)) return false;
+        const ImageInfo& info = src.info();
+        r2p_image img;
+        std::memset(&img, 0, sizeof(img));
+        img.width = info.width;
+        img.height = info.height;
+        img.channels = info.channels;
+        img.bytes_per_sample = info.bits_per_sample / 8;
+        img.window_mode = mode;
+        std::memcpy(&img.dicom, src.dicom_params(), sizeof(img.dicom));
+        return r2p_host::write_bmp(img, src.pixel_data_.data(), out.c_str(), cfg.device);
     };
 
     // a TIFF file: samples already in PNG order, no window
@@ -189,7 +206,8 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
             const std::string stem = files[i].stem().string();
             DicomSource src;
             if (is_tiff_file(path.c_str())) {
-                job.ok = submit_tiff(path, (outdir / (stem + ".png")).string(), job);
+                job.ok = bmp ? encode_tiff_to_bmp(path.c_str(), (outdir / (stem + ext)).string().c_str(), cfg)
+                             : submit_tiff(path, (outdir / (stem + ext)).string(), job);
             } else if (!is_dicom_file(path.c_str())) {
                 std::fprintf(stderr, "%s: camera RAW input is not part of this build\n", path.c_str());
                 job.ok = false;
@@ -209,8 +227,9 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
                 const ImageInfo& info = src.info();
                 const int mode = (info.channels == 1 && info.bits_per_sample == 16) ? R2P_WINDOW_BATCH8
                                                                                     : R2P_WINDOW_DICOM16;
+                const std::string out = (outdir / (stem + ext)).string();
                 job.ok = frame < src.num_frames() &&
-                         submit_frame(src, frame, mode, (outdir / (stem + ".png")).string(), job);
+                         (bmp ? write_frame_bmp(src, frame, mode, out) : submit_frame(src, frame, mode, out, job));
             }
             std::lock_guard<std::mutex> lk(mu);
             jobs[i] = std::move(job);

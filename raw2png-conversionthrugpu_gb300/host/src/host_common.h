@@ -40,4 +40,8 @@ inline bool split_bpp(int bpp, int bytes_per_sample, int& channels, int& bps)
 // src/pipeline.cpp:1522-1560).
 r2p_engine* thread_engine(int device);
 
+// BMP file of host pixels through r2p_encode_bmp on the calling thread's
+// engine, written to `out`.
+bool write_bmp(const r2p_image& img, const void* pixels, const char* out, int device);
+
 }  // namespace r2p_host

@@ -37,7 +37,8 @@ static void usage(const char* prog)
                  "  --batch-verbose      per-file wall time in folder mode\n"
                  "  --gpu-streams N      frames in flight for --all (default 4)\n"
                  "  --gpu-deflate, --gpu-lz77, --no-gpu-lz77, --gpu-lz77-debug   accepted (always GPU)\n"
-                 "  --format png         (bmp is not part of this build)\n"
+                 "  --format png|bmp     output format (default png); bmp: uncompressed 8-bit gray /\n"
+                 "                       24-bit BGR, written on the GPU\n"
                  "  --strip-pipeline     run strips through gpu_filter + GpuDeflateBackend\n"
                  "  --idat-chunk N       IDAT chunks of at most N bytes (default: one IDAT)\n"
                  "  --device N           GPU ordinal\n"
@@ -124,7 +125,7 @@ int main(int argc, char* argv[])
             if (!std::strcmp(f, "png") || !std::strcmp(f, "PNG")) cfg.format = ExportFormat::PNG;
             else if (!std::strcmp(f, "bmp") || !std::strcmp(f, "BMP")) cfg.format = ExportFormat::BMP;
             else {
-                std::fprintf(stderr, "Unknown format '%s'. Supported: png\n", f);
+                std::fprintf(stderr, "Unknown format '%s'. Supported: png, bmp\n", f);
                 return 1;
             }
         } else {
@@ -136,9 +137,10 @@ int main(int argc, char* argv[])
     if (cfg.deflate_level < 0) cfg.deflate_level = 0;
     if (cfg.deflate_level > 9) cfg.deflate_level = 9;
     if (cfg.strip_height < 0) cfg.strip_height = 0;
-    if (cfg.format == ExportFormat::BMP) {
-        std::fprintf(stderr, "BMP export is not part of this build\n");
-        return 1;
+    const bool use_bmp = cfg.format == ExportFormat::BMP;
+    if (all_frames && use_bmp) {      // src/main.cpp:210-214
+        std::fprintf(stderr, "Note: --all applies only to DICOM PNG mode; ignoring.\n");
+        all_frames = false;
     }
     std::error_code ec;
     if (std::filesystem::is_directory(input, ec)) {
@@ -149,7 +151,10 @@ int main(int argc, char* argv[])
         return 0;
     }
     bool good;
-    if (is_tiff_file(input)) good = encode_tiff_to_png(input, output, cfg);
+    if (use_bmp) good = is_tiff_file(input)  ? encode_tiff_to_bmp(input, output, cfg)
+                      : is_raw_file(input)   ? encode_raw_to_bmp(input, output, cfg)
+                                             : encode_dicom_to_bmp(input, output, cfg);
+    else if (is_tiff_file(input)) good = encode_tiff_to_png(input, output, cfg);
     else if (is_raw_file(input)) good = encode_raw_to_png(input, output, cfg);
     else if (all_frames) good = encode_dicom_all_frames_to_png(input, output, cfg);
     else good = encode_dicom_to_png(input, output, cfg);

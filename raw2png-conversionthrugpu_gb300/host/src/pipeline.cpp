@@ -69,6 +69,29 @@ struct PinnedScratch {
     }
 };
 
+bool write_bmp(const r2p_image& img, const void* pixels, const char* out, int device)
+{
+    thread_local PinnedScratch bmp_buf;
+    const size_t size = r2p_bmp_bound(&img);
+    if (size == 0) {
+        std::fprintf(stderr, "BMP: unsupported image %ux%u, %d channel(s), %d byte(s) per sample\n", img.width,
+                     img.height, img.channels, img.bytes_per_sample);
+        return false;
+    }
+    uint8_t* bmp = bmp_buf.get(size);
+    r2p_engine* eng = thread_engine(device);
+    if (!bmp || !eng) return false;
+    size_t len = 0;
+    if (!ok(r2p_encode_bmp(eng, &img, pixels, bmp, size, &len), "r2p_encode_bmp")) return false;
+    FILE* f = std::fopen(out, "wb");
+    if (!f) {
+        std::fprintf(stderr, "Cannot create BMP: %s\n", out);
+        return false;
+    }
+    const bool good = std::fwrite(bmp, 1, len, f) == len;
+    return (std::fclose(f) == 0) && good;
+}
+
 }  // namespace r2p_host
 
 using namespace r2p_host;
@@ -243,10 +266,30 @@ bool encode_source_to_png(ImageSource& src, const char* output_path, const Pipel
     return whole ? encode_whole(src, output_path, cfg, img) : encode_strips(src, output_path, cfg, img);
 }
 
-bool encode_source_to_bmp(ImageSource&, const char*)
+namespace {
+
+// The reference's BMP export of a source (run_bmp_from_source,
+// src/pipeline.cpp:1944-2004) on the GPU: DICOM sources through the BMP
+// path's own 16-bit gray window, others by the first byte of 16-bit samples
+// or as they are.
+bool bmp_from_source(ImageSource& src, const char* out, int device)
 {
-    std::fprintf(stderr, "BMP export is not part of this build\n");
-    return false;
+    thread_local PinnedScratch raw_buf;
+    const ImageInfo& info = src.info();
+    PipelineConfig cfg;
+    r2p_image img;
+    if (!describe(src, cfg, img)) return false;
+    const size_t rb = (size_t)info.width * info.bpp;
+    uint8_t* raw = raw_buf.get(rb * info.height);
+    if (!raw || !read_all(src, raw, 64, rb)) return false;
+    return write_bmp(img, raw, out, device);
+}
+
+}  // namespace
+
+bool encode_source_to_bmp(ImageSource& src, const char* output_path)
+{
+    return bmp_from_source(src, output_path, 0);
 }
 
 bool encode_tiff_to_png(const char* input_path, const char* output_path, const PipelineConfig& cfg)
@@ -269,20 +312,36 @@ bool encode_raw_to_png(const char* input_path, const char*, const PipelineConfig
     return false;
 }
 
-bool encode_dicom_to_bmp(const char*, const char*, const PipelineConfig&)
+bool encode_dicom_to_bmp(const char* input_path, const char* output_path, const PipelineConfig& cfg)
 {
-    std::fprintf(stderr, "BMP export is not part of this build\n");
+    DicomSource src;
+    if (!src.open(input_path)) {
+        std::fprintf(stderr, "Cannot open DICOM: %s\n", input_path);
+        return false;
+    }
+    const int frame = cfg.frame >= 0 ? cfg.frame : 0;
+    if (frame >= src.num_frames()) {
+        std::fprintf(stderr, "DICOM: requested frame %d but file has %d frame(s)\n", frame, src.num_frames());
+        return false;
+    }
+    if (!src.load_frame(frame)) return false;
+    return bmp_from_source(src, output_path, cfg.device);
+}
+
+bool encode_tiff_to_bmp(const char* input_path, const char* output_path, const PipelineConfig& cfg)
+{
+    TiffSource src;
+    if (!src.open(input_path)) {
+        std::fprintf(stderr, "Cannot open TIFF: %s\n", input_path);
+        return false;
+    }
+    return bmp_from_source(src, output_path, cfg.device);
+}
+
+bool encode_raw_to_bmp(const char* input_path, const char*, const PipelineConfig&)
+{
+    std::fprintf(stderr, "camera RAW input is not part of this build: %s\n", input_path);
     return false;
-}
-
-bool encode_tiff_to_bmp(const char* p, const char* o, const PipelineConfig& c)
-{
-    return encode_dicom_to_bmp(p, o, c);
-}
-
-bool encode_raw_to_bmp(const char* p, const char* o, const PipelineConfig& c)
-{
-    return encode_dicom_to_bmp(p, o, c);
 }
 
 bool encode_dicom_to_png(const char* input_path, const char* output_path, const PipelineConfig& cfg)

@@ -175,3 +175,44 @@ def test_folder_with_tiff(cli, O, W, tmp_path):
     check_png(O, dst / "photo.png", T.expected_png_bytes(img), 8, 2)
     want, _ = O.window8(px.view(np.uint8), O.make_params(16, 12, 11, 0, slope=1.0, intercept=-1024.0, wc=40.0, ww=400.0))
     check_png(O, dst / "ct.png", want, 8, 0)
+
+
+# ---- BMP export (--format bmp): the reference's BMP path, written on the GPU
+def test_bmp_single_files(cli, O, W, tmp_path):
+    px = W.ct_phantom(4, 301, 97)
+    f = tmp_path / "ct.dcm"
+    D.write_dicom(f, px, bits_stored=12, high_bit=11, slope=1.0, intercept=-1024.0, wc=40.0, ww=400.0)
+    out = tmp_path / "ct.bmp"
+    run(cli, f, out, "--format", "bmp", "--all")                    # --all is ignored for BMP
+    p = params(O, slope=1.0, intercept=-1024.0, wc=40.0, ww=400.0)
+    assert out.read_bytes() == O.bmp_file(px.view(np.uint8), 301, 97, 1, 2, "dicom", p)
+    rgb = np.random.default_rng(5).integers(0, 65536, size=(23, 37, 3), dtype=np.uint16)
+    t = tmp_path / "rgb.tif"
+    T.write_tiff(t, rgb, order="MM")
+    out = tmp_path / "rgb.bmp"
+    run(cli, t, out, "--format", "BMP")
+    assert out.read_bytes() == O.bmp_file(T.expected_png_bytes(rgb), 37, 23, 3, 2, "be")
+
+
+def test_bmp_folder(cli, O, W, tmp_path):
+    src, dst = tmp_path / "in", tmp_path / "out"
+    src.mkdir()
+    ct = W.ct_phantom(6, 128, 96)
+    D.write_dicom(src / "a.dcm", ct, bits_stored=12, high_bit=11, slope=1.0, intercept=-1024.0, wc=40.0, ww=100.0)
+    u8 = np.random.default_rng(6).integers(0, 256, size=(1, 33, 45), dtype=np.uint8)
+    D.write_dicom(src / "b.dcm", u8, bits_allocated=8, bits_stored=8, high_bit=7)
+    frames = np.random.default_rng(7).integers(0, 4096, size=(2, 20, 30), dtype=np.uint16)
+    D.write_dicom(src / "c.dcm", frames, wc=2048.0, ww=4096.0)
+    g = np.random.default_rng(8).integers(0, 65536, size=(17, 29), dtype=np.uint16)
+    T.write_tiff(src / "d.tif", g)
+    run(cli, src, dst, "--format", "bmp", "--level", 1)
+    p = params(O, slope=1.0, intercept=-1024.0, wc=40.0, ww=100.0)
+    # 16-bit grayscale: the batch 16->8 rule, then an 8-bit BMP
+    assert (dst / "a.bmp").read_bytes() == O.bmp_file(ct.view(np.uint8), 128, 96, 1, 2, "batch8", p)
+    assert (dst / "b.bmp").read_bytes() == O.bmp_file(u8.reshape(-1), 45, 33, 1, 1, "dicom",
+                                                        params(O, 8, 7, ba=8))
+    assert (dst / "d.bmp").read_bytes() == O.bmp_file(T.expected_png_bytes(g), 29, 17, 1, 2, "be")
+    # multi-frame files stay PNG slices, as in the reference
+    pf = params(O, wc=2048.0, ww=4096.0)
+    for i in range(2):
+        check_png(O, dst / "c" / ("slice_%04d.png" % i), O.window_a2(frames[i].view(np.uint8).reshape(-1), pf), 16, 0)

@@ -174,3 +174,37 @@ def test_filter_pinned_to_reference_kernel(O):
                               d["flt_%d_fm" % k])
         seen_types.update(int(t) for t in want.reshape(rows, wb + 1)[:, 0])
     assert seen_types == {0, 1, 2, 3, 4}, "the recorded strips exercise every filter type"
+
+
+# tests/golden/bmp_ref.npz holds BMP files written by the reference's own BMP
+# export (encode_source_to_bmp: src/pipeline.cpp:1944-2004 with
+# src/bmp_writer.cpp) for seeded images; tests/golden/gen_bmp_golden.py made
+# them with oracle/_ref/ref_bmp_runner.
+def bmp_golden(O):
+    d = np.load(os.path.join(GOLDEN, "bmp_ref.npz"))
+    cases = []
+    for i, m in enumerate(json.loads(str(d["meta"]))):
+        p = None
+        if m["params"]:
+            p = O.OrcParams()
+            for k, v in m["params"].items():
+                setattr(p, k, v)
+        cases.append((m, p, d["raw_%d" % i], d["bmp_%d" % i].tobytes()))
+    return cases
+
+
+def test_bmp_pinned_to_reference_export(O):
+    cases = bmp_golden(O)
+    assert len(cases) >= 20
+    for m, p, raw, want in cases:
+        got = O.bmp_file(raw, m["width"], m["height"], m["channels"], m["bytes_per_sample"], m["mode"], p)
+        assert got == want, m["name"]
+
+
+def test_bmp_window_divides_by_the_range(O):
+    # the BMP formula and the batch table differ only in (val-lo)/(hi-lo)
+    # versus (val-lo)*(1/(hi-lo)); at WC 2000 / WW 3000 they round apart
+    ramp = np.arange(4096, dtype="<u2").view(np.uint8)
+    p = O.make_params(16, 12, None, 0, None, None, 2000.0, 3000.0)
+    a, b = O.bmp_gray8(ramp, p), O.build_lut(p)
+    assert np.flatnonzero(a != b).tolist() == [600, 1400]
