@@ -4,8 +4,9 @@
 // checksums and PNG container on the GPU); with strip_pipeline set, or for
 // images beyond one call's limit, strips run through gpu_filter_* and
 // GpuDeflateBackend into a PngWriter, as the reference's pipeline does.
-// TIFF, camera-RAW and BMP paths are not part of this build and report an
-// error.
+// BMP export (encode_*_to_bmp) writes the whole file on the GPU through
+// r2p_encode_bmp, in the reference's BMP layout and pixel rules.  Camera-RAW
+// input is not part of this build and reports an error.
 #include <cstdint>
 
 struct ImageSource;
