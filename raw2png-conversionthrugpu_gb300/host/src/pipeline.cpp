@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "bounded_queue.h"
 #include "compression_backend.h"
 #include "dicom_loader.h"
 #include "gpu_filter.h"
@@ -190,11 +191,21 @@ bool encode_whole(ImageSource& src, const char* out, const PipelineConfig& cfg, 
     return (std::fclose(f) == 0) && good;
 }
 
+// Strip path as three overlapped stages, like the reference's modern
+// pipeline (src/pipeline.cpp:445-853): a reader thread fills a ring of pinned
+// strip buffers from the source, this thread runs each strip through the GPU
+// filter (prior row carried on the device) and GpuDeflateBackend, and a
+// writer thread appends the compressed strips to the PNG's IDAT chunks
+// (modern_writer_stage, :826-848), so source reads and file writes overlap
+// the GPU work.
 bool encode_strips(ImageSource& src, const char* out, const PipelineConfig& cfg, const r2p_image& img)
 {
+    constexpr int kRing = 3;                      // strip buffers in flight
     const ImageInfo& info = src.info();
+    const int H = (int)info.height;
     const int strip = strip_rows(cfg);
     const size_t rb = (size_t)info.width * info.bpp;
+    const size_t slot_bytes = (size_t)strip * rb;
     const DicomPixelParams* dicom = src.dicom_params();
     GpuFilterContext* ctx = gpu_filter_create((int)info.width, info.bpp, strip, true);
     if (!ctx) return false;
@@ -202,45 +213,81 @@ bool encode_strips(ImageSource& src, const char* out, const PipelineConfig& cfg,
     dc.num_threads = cfg.deflate_threads;
     dc.zlib_level = img.level;
     GpuDeflateBackend backend(dc, cfg.device);
-    thread_local PinnedScratch strip_buf;
-    uint8_t* buf = strip_buf.get((size_t)strip * rb);
+    thread_local PinnedScratch ring_buf;
+    uint8_t* ring = ring_buf.get(kRing * slot_bytes);
     PngWriter w;
     if (cfg.idat_chunk > 0) w.set_idat_chunk((size_t)cfg.idat_chunk);
-    bool good = buf && backend.ok() &&
+    bool good = ring && backend.ok() &&
                 w.open(out, info.width, info.height, (uint8_t)info.bits_per_sample, color_type(info.channels));
     if (good) {
         w.begin_idat();
         uint8_t hdr[2];
         zlib_header(img.level, hdr);
         w.write_idat_bytes(hdr, 2);
+        struct StripIn {
+            int slot = 0, rows = 0;
+        };
+        BoundedQueue<int> q_free(kRing);
+        BoundedQueue<StripIn> q_in(kRing);
+        BoundedQueue<std::vector<uint8_t>> q_out(kRing + 1);
+        for (int k = 0; k < kRing; k++) q_free.push(k);
+        std::atomic<bool> failed{false};
+        std::thread reader([&] {
+            for (int r = 0; r < H;) {
+                int slot;
+                if (!q_free.pop(slot)) break;
+                const int n = src.read_strip(ring + slot * slot_bytes, std::min(strip, H - r));
+                if (n <= 0) {
+                    std::fprintf(stderr, "encode: source ended at row %d of %d\n", r, H);
+                    failed = true;
+                    break;
+                }
+                StripIn si;
+                si.slot = slot;
+                si.rows = n;
+                if (!q_in.push(si)) break;
+                r += n;
+            }
+            q_in.close();
+        });
+        std::thread writer([&] {
+            std::vector<uint8_t> b;
+            while (q_out.pop(b))
+                if (!failed) w.write_idat_bytes(b.data(), b.size());
+        });
         ParallelDeflateState st;
         gpu_filter_reset(ctx);
-        for (int r = 0; good && r < (int)info.height;) {
-            const int n = src.read_strip(buf, std::min(strip, (int)info.height - r));
-            if (n <= 0) {
-                std::fprintf(stderr, "encode: source ended at row %d of %u\n", r, info.height);
-                good = false;
-                break;
-            }
-            gpu_filter_process_from_host(ctx, buf, nullptr, n, nullptr, dicom, true);
-            const bool last = r + n == (int)info.height;
+        int done = 0;
+        StripIn si;
+        while (!failed && q_in.pop(si)) {
+            gpu_filter_process_from_host(ctx, ring + si.slot * slot_bytes, nullptr, si.rows, nullptr, dicom, true);
+            const bool last = done + si.rows == H;
+            // waits for the strip's stream: the upload from the slot is done after this
             DeflateResult dr = backend.compress_strip_device(gpu_filter_device_output(ctx),
-                                                             gpu_filter_output_size(ctx, n), last,
+                                                             gpu_filter_output_size(ctx, si.rows), last,
                                                              gpu_filter_stream(ctx));
+            q_free.push(si.slot);
             if (dr.data.empty()) {
-                good = false;
+                failed = true;
                 break;
             }
             accum_adler(st, dr);
-            w.write_idat_bytes(dr.data.data(), dr.data.size());
-            r += n;
+            q_out.push(std::move(dr.data));
+            done += si.rows;
         }
-        if (good) {
-            uint8_t trl[4];
-            zlib_trailer(st, trl);
-            w.write_idat_bytes(trl, 4);
-            w.end_idat();
+        if (done != H) failed = true;
+        q_free.close();
+        q_in.close();
+        reader.join();
+        if (!failed) {
+            std::vector<uint8_t> trl(4);
+            zlib_trailer(st, trl.data());
+            q_out.push(std::move(trl));
         }
+        q_out.close();
+        writer.join();
+        good = !failed;
+        if (good) w.end_idat();
         w.close();
         good = good && !w.failed();
     }

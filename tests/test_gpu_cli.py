@@ -216,3 +216,15 @@ def test_bmp_folder(cli, O, W, tmp_path):
     pf = params(O, wc=2048.0, ww=4096.0)
     for i in range(2):
         check_png(O, dst / "c" / ("slice_%04d.png" % i), O.window_a2(frames[i].view(np.uint8).reshape(-1), pf), 16, 0)
+
+
+def test_strip_pipeline_many_strips(cli, O, W, tmp_path):
+    # 33 strips through the three-slot reader ring and the writer thread
+    px = W.ct_phantom(11, 173, 263)
+    f = tmp_path / "ct.dcm"
+    D.write_dicom(f, px, bits_stored=12, high_bit=11, wc=40.0, ww=400.0, slope=1.0, intercept=-1024.0)
+    out = tmp_path / "ct.png"
+    run(cli, f, out, "--level", 1, "--strip-pipeline", "--strip-height", 8, "--idat-chunk", 4096)
+    want = O.window_a2(px.view(np.uint8), params(O, slope=1.0, intercept=-1024.0, wc=40.0, ww=400.0))
+    _, filt = check_png(O, out, want, 16, 0, 4096)
+    assert np.array_equal(filt, O.filter_rows(want, 263, 346, 2))
