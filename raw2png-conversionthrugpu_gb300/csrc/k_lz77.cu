@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include "k_deflate.cuh"
+#include "r2p_huff.h"
 #include "r2p_kernels.h"
 
 namespace r2p {
@@ -271,7 +272,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
         BlockOut& bo = blocks[b];
         const DevImage& d = imgs[bo.img];
-        if (d.level == 0) continue;
+        if (d.level != 1) continue;                 // level 0: stored; >= 2: dynamic blocks
         const int n = (int)bo.in_len;
         const uint8_t* src = d.filt + bo.in_off;
         const bool last = ((int)(b - d.blk0) == d.nblocks - 1) && !d.open_end;
@@ -375,6 +376,375 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             bo.s2 = s2;
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Levels 2-9: dynamic-Huffman blocks (BTYPE = 10) over a run-length parse.
+//
+// Filtered scanlines are mostly small residuals and runs; coding them with a
+// per-block Huffman code (RFC 1951 3.2.7) matters far more than a match
+// search (zlib's run-length strategy, distance-1 matches only, is what PNG
+// encoders use for this data).  One 256-thread CTA per block, two per SM:
+//   1. stage the block; each thread parses its sub-range (tokens: a literal,
+//      or a run of 3..258 copies of the previous byte = length, distance 1)
+//      into per-warp symbol histograms;
+//   2. one thread builds the literal/length code (lengths <= 15, r2p_huff.h),
+//      the canonical codes and the block header, and sizes the block; the
+//      block is stored instead when that is smaller;
+//   3. every thread re-parses to count its bits, a CTA scan gives each its
+//      bit offset, and a third parse writes its codes straight into the
+//      block's slot (shared atomics only for the words at stream ends);
+//   4. end-of-block code, the empty stored block of non-final blocks, CRC.
+// ---------------------------------------------------------------------------
+constexpr int kDynThreads = 256;
+constexpr int kDynWarps = kDynThreads / 32;
+
+// Bytes per thread: a multiple of 4 with an odd word count (distinct banks).
+__host__ __device__ inline int dyn_sub_bytes(int block_size)
+{
+    const int w = ((block_size + kDynThreads - 1) / kDynThreads + 3) >> 2;
+    return 4 * (w | 1);
+}
+
+struct DynLayout {
+    int in, hist, freq, wt, lt, sorted, lltab, lens, codes, hw, lsym, total;
+};
+
+__host__ __device__ inline DynLayout dyn_layout(int max_block)
+{
+    DynLayout L;
+    int o = 4096;                                   // CRC tables
+    L.in = o;     o += lz_in_bytes(max_block);
+    L.hist = o;   o += kDynWarps * kLLSyms * 4;
+    L.freq = o;   o += kLLSyms * 4;
+    L.wt = o;     o += kLLSyms * 4;
+    L.lt = o;     o += kLLSyms * 4;
+    L.sorted = o; o += ((kLLSyms * 2 + 15) & ~15);
+    L.lltab = o;  o += kLLSyms * 4;
+    L.lens = o;   o += ((kLLSyms + kDSyms + 15) & ~15);
+    L.codes = o;  o += (((kLLSyms + kDSyms) * 2 + 15) & ~15);
+    L.hw = o;     o += kHdrWords * 4;
+    L.lsym = o;   o += 256 * 4;
+    L.total = o;
+    return L;
+}
+
+// Run-length parse of in[s, e): calls f.lit(byte) or f.match(len 3..258).
+template <class F>
+__device__ __forceinline__ void rle_parse(const uint8_t* in, int s, int e, F& f)
+{
+    uint32_t prev = s > 0 ? (uint32_t)in[s - 1] : 0x100u;   // no run at the block start
+    int p = s;
+    while (p < e) {
+        const uint32_t b = in[p];
+        if (b == prev) {
+            const int maxl = min(kMaxMatch, e - p);
+            const uint32_t pat = prev * 0x01010101u;
+            int L = 1;
+            bool more = true;
+            while (more && L + 4 <= maxl) {
+                const uint32_t x = ld32u(in, p + L) ^ pat;
+                if (x) {
+                    L += (__ffs(x) - 1) >> 3;
+                    more = false;
+                } else {
+                    L += 4;
+                }
+            }
+            while (more && L < maxl && in[p + L] == prev) L++;
+            if (L >= 3) {
+                f.match(L);
+                p += L;
+                continue;
+            }
+        }
+        f.lit(b);
+        prev = b;
+        p++;
+    }
+}
+
+// lsym[len - 3] = length symbol | extra bit count << 9 | extra value << 12
+struct RleHist {
+    uint32_t* h;
+    const uint32_t* lsym;
+    uint32_t matches, extra;
+    __device__ void lit(uint32_t b) { atomicAdd(&h[b], 1u); }
+    __device__ void match(int L)
+    {
+        const uint32_t e = lsym[L - 3];
+        atomicAdd(&h[e & 511u], 1u);
+        matches++;
+        extra += (e >> 9) & 7u;
+    }
+};
+
+// tab[sym] = reversed code | length << 16
+struct RleCount {
+    const uint32_t* tab;
+    const uint32_t* lsym;
+    uint32_t dlen, bits;
+    __device__ void lit(uint32_t b) { bits += tab[b] >> 16; }
+    __device__ void match(int L)
+    {
+        const uint32_t e = lsym[L - 3];
+        bits += (tab[e & 511u] >> 16) + ((e >> 9) & 7u) + dlen;
+    }
+};
+
+// Writes a thread's codes from bit `off` of the zeroed output words: whole
+// words by plain stores, the first (when it starts mid-word) and the last
+// partial word by atomicOr, as the neighbouring streams share them.
+struct RleEmit {
+    const uint32_t* tab;
+    const uint32_t* lsym;
+    uint32_t dcode, dlen;
+    uint32_t* out;
+    uint64_t acc;
+    uint32_t nacc, q, q_first;
+    bool first_shared;
+    __device__ void init(uint32_t* o, uint32_t off)
+    {
+        out = o;
+        acc = 0;
+        nacc = off & 31u;
+        q = q_first = off >> 5;
+        first_shared = nacc != 0;
+    }
+    __device__ void put(uint32_t v, uint32_t n)
+    {
+        acc |= (uint64_t)v << nacc;
+        nacc += n;
+        if (nacc >= 32u) {
+            const uint32_t w = (uint32_t)acc;
+            if (q == q_first && first_shared) atomicOr(out + q, w);
+            else out[q] = w;
+            q++;
+            acc >>= 32;
+            nacc -= 32u;
+        }
+    }
+    __device__ void lit(uint32_t b)
+    {
+        const uint32_t t = tab[b];
+        put(t & 0xFFFFu, t >> 16);
+    }
+    __device__ void match(int L)
+    {
+        const uint32_t e = lsym[L - 3];
+        const uint32_t t = tab[e & 511u];
+        put(t & 0xFFFFu, t >> 16);
+        const uint32_t ne = (e >> 9) & 7u;
+        if (ne) put(e >> 12, ne);
+        put(dcode, dlen);
+    }
+    __device__ void finish()
+    {
+        if (nacc > 0) atomicOr(out + q, (uint32_t)acc);    // the next stream may start in this word
+    }
+};
+
+// OR n <= 25 bits into global words at bit pos (words shared with other writers).
+__device__ __forceinline__ void or_bits_global(uint32_t* w, uint32_t pos, uint32_t v, uint32_t n)
+{
+    const uint32_t q = pos >> 5, sh = pos & 31u;
+    atomicOr(w + q, v << sh);
+    if (sh + n > 32u) atomicOr(w + q + 1, v >> (32u - sh));
+}
+
+__global__ void __launch_bounds__(kDynThreads)
+k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int max_block,
+                 uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
+{
+    extern __shared__ __align__(16) uint8_t sm[];
+    const DynLayout Ly = dyn_layout(max_block);
+    uint32_t (*ctab)[256] = reinterpret_cast<uint32_t (*)[256]>(sm);
+    uint8_t* in = sm + Ly.in;
+    const int in_bytes = lz_in_bytes(max_block);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(sm + Ly.hist);
+    uint32_t* freq = reinterpret_cast<uint32_t*>(sm + Ly.freq);
+    uint32_t* wt = reinterpret_cast<uint32_t*>(sm + Ly.wt);
+    uint32_t* lt = reinterpret_cast<uint32_t*>(sm + Ly.lt);
+    uint16_t* sorted = reinterpret_cast<uint16_t*>(sm + Ly.sorted);
+    uint32_t* lltab = reinterpret_cast<uint32_t*>(sm + Ly.lltab);
+    uint8_t* ll_len = sm + Ly.lens;
+    uint8_t* d_len = ll_len + kLLSyms;
+    uint16_t* ll_code = reinterpret_cast<uint16_t*>(sm + Ly.codes);
+    uint16_t* d_code = ll_code + kLLSyms;
+    uint32_t* hw = reinterpret_cast<uint32_t*>(sm + Ly.hw);
+    uint32_t* lsym = reinterpret_cast<uint32_t*>(sm + Ly.lsym);
+    __shared__ uint64_t red64[kDynWarps];
+    __shared__ uint32_t red32[kDynWarps];
+    __shared__ uint32_t wsum[kDynWarps];
+    __shared__ uint32_t s_info[4];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    build_crc_tables(ctab);
+    for (int i = tid; i < 256; i += kDynThreads) {
+        int sym, ne, ex;
+        length_symbol(i + 3, sym, ne, ex);
+        lsym[i] = (uint32_t)sym | ((uint32_t)ne << 9) | ((uint32_t)ex << 12);
+    }
+
+    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        BlockOut& bo = blocks[b];
+        const DevImage& d = imgs[bo.img];
+        if (d.level < 2) continue;
+        const int n = (int)bo.in_len;
+        const uint8_t* src = d.filt + bo.in_off;
+        const bool last = ((int)(b - d.blk0) == d.nblocks - 1) && !d.open_end;
+        __syncthreads();
+        if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+            for (int i = tid; i < (n >> 4); i += kDynThreads)
+                reinterpret_cast<uint4*>(in)[i] = __ldg(reinterpret_cast<const uint4*>(src) + i);
+            for (int i = (n & ~15) + tid; i < n; i += kDynThreads) in[i] = src[i];
+        } else {
+            for (int i = tid; i < n; i += kDynThreads) in[i] = src[i];
+        }
+        for (int i = n + tid; i < in_bytes; i += kDynThreads) in[i] = 0;
+        for (int i = tid; i < kDynWarps * kLLSyms; i += kDynThreads) hist[i] = 0u;
+        for (int i = tid; i < kLLSyms + kDSyms; i += kDynThreads) ll_len[i] = 0;
+        __syncthreads();
+        uint32_t s1;
+        uint64_t s2;
+        cta_adler_sums<kDynThreads>(in, n, s1, s2, red64);
+        const int sub = dyn_sub_bytes(n);
+        const int s = min(n, tid * sub), e = min(n, s + sub);
+        // 1. histogram
+        RleHist H{hist + warp * kLLSyms, lsym, 0u, 0u};
+        rle_parse(in, s, e, H);
+        const uint32_t matches = (uint32_t)cta_sum64<kDynThreads>(H.matches, red64);
+        const uint64_t extra = cta_sum64<kDynThreads>(H.extra, red64);
+        for (int i = tid; i < kLLSyms; i += kDynThreads) {
+            uint32_t f = (i == 256) ? 1u : 0u;        // one end-of-block code
+            for (int w = 0; w < kDynWarps; w++) f += hist[w * kLLSyms + i];
+            freq[i] = f;
+        }
+        __syncthreads();
+        // 2. used symbols sorted by (frequency, symbol): each thread ranks its own
+        for (int i = tid; i < kLLSyms; i += kDynThreads) {
+            const uint32_t f = freq[i];
+            if (!f) continue;
+            int r = 0;
+            for (int j = 0; j < kLLSyms; j++) {
+                const uint32_t g = freq[j];
+                r += (g && (g < f || (g == f && j < i))) ? 1 : 0;
+            }
+            sorted[r] = (uint16_t)i;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int nu = 0;
+            for (int i = 0; i < kLLSyms; i++) nu += freq[i] ? 1 : 0;
+            for (int i = 0; i < nu; i++) wt[i] = freq[sorted[i]];
+            if (nu >= 2) limited_lengths(wt, nu, kMaxCodeLen, lt);
+            else lt[0] = 1;                            // (a block always has a literal and the end code)
+            s_info[3] = (uint32_t)nu;
+        }
+        __syncthreads();
+        const int nu = (int)s_info[3];
+        for (int i = tid; i < nu; i += kDynThreads) ll_len[sorted[i]] = (uint8_t)lt[i];
+        __syncthreads();
+        if (tid == 0) {
+            d_len[0] = matches ? 1 : 0;
+            canonical_codes(ll_len, kLLSyms, ll_code);
+            canonical_codes(d_len, kDSyms, d_code);
+            for (int k = 0; k < kHdrWords; k++) hw[k] = 0u;
+            uint32_t pos = 0;
+            put_bits(hw, pos, last ? 5u : 4u, 3);      // BFINAL, BTYPE = 10
+            const uint32_t hend = build_dyn_header(ll_len, d_len, hw, pos);
+            uint64_t body = 0;
+            for (int i = 0; i < kLLSyms; i++) body += (uint64_t)freq[i] * ll_len[i];
+            const uint64_t total = hend + body + extra + (uint64_t)matches * d_len[0];
+            const uint64_t dyn = last ? (total + 7) / 8 : (total + 3 + 7) / 8 + 4;
+            s_info[0] = (dyn < (uint64_t)(n + kStoredHdr)) ? (uint32_t)dyn : 0u;   // 0 = stored block
+            s_info[1] = hend;
+            s_info[2] = (uint32_t)total;
+        }
+        __syncthreads();
+        for (int i = tid; i < kLLSyms; i += kDynThreads) lltab[i] = (uint32_t)ll_code[i] | ((uint32_t)ll_len[i] << 16);
+        const uint32_t dyn = s_info[0];
+        uint8_t* slot = scratch + (size_t)b * slot_bytes;
+        uint32_t crc;
+        if (dyn) {
+            const uint32_t hend = s_info[1], total = s_info[2];
+            uint32_t* out = reinterpret_cast<uint32_t*>(slot);
+            const int owords = (int)((dyn + 3) / 4) + 1;
+            for (int i = tid; i < owords; i += kDynThreads) out[i] = 0u;
+            __syncthreads();
+            // 3. bit counts, offsets, codes
+            RleCount C{lltab, lsym, (uint32_t)d_len[0], 0u};
+            rle_parse(in, s, e, C);
+            uint32_t incl = C.bits;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) wsum[warp] = incl;
+            if (tid == 0)
+                for (int k = 0; k < (int)((hend + 31) / 32); k++) out[k] = hw[k];
+            __syncthreads();
+            uint32_t wbase = 0;
+            for (int k = 0; k < warp; k++) wbase += wsum[k];
+            RleEmit E;
+            E.tab = lltab;
+            E.lsym = lsym;
+            E.dcode = d_code[0];
+            E.dlen = d_len[0];
+            E.init(out, hend + wbase + incl - C.bits);
+            rle_parse(in, s, e, E);
+            E.finish();
+            __syncthreads();
+            if (tid == 0) {
+                const uint32_t eob = lltab[256];
+                or_bits_global(out, total - (eob >> 16), eob & 0xFFFFu, eob >> 16);
+                if (!last) {                               // empty stored block: 3 zero bits, pad, 0000 FFFF
+                    const uint32_t k = (total + 3 + 7) / 8;
+                    slot[k + 2] = 0xFF;
+                    slot[k + 3] = 0xFF;
+                }
+            }
+            __syncthreads();
+            uint32_t s1d;
+            uint64_t s2d;
+            cta_crc_adler<kDynThreads>(slot, (int)dyn, false, ctab, xpow, crc, s1d, s2d, red64, red32);
+        } else {
+            uint8_t hdr[kStoredHdr] = {(uint8_t)(last ? 1 : 0), (uint8_t)(n & 0xFF), (uint8_t)(n >> 8),
+                                       (uint8_t)(~n & 0xFF), (uint8_t)((~n >> 8) & 0xFF)};
+            if (tid < kStoredHdr) slot[tid] = hdr[tid];
+            cta_copy_to_global<kDynThreads>(slot + kStoredHdr, in, n);
+            uint32_t cd, s1d;
+            uint64_t s2d;
+            cta_crc_adler<kDynThreads>(in, n, false, ctab, xpow, cd, s1d, s2d, red64, red32);
+            crc = gf2_mulmod(crc_small(hdr, kStoredHdr, ctab), xpow8n((uint64_t)n, xpow)) ^ cd;
+        }
+        if (tid == 0) {
+            bo.out_len = dyn ? dyn : (uint32_t)(n + kStoredHdr);
+            bo.crc = crc;
+            bo.s1 = s1;
+            bo.s2 = s2;
+        }
+    }
+}
+
+int dyn_ctas_per_sm(int max_block)
+{
+    int n = 0;
+    const int smem = dyn_layout(max_block).total;
+    cudaFuncSetAttribute(k_rle_dyn_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rle_dyn_blocks, kDynThreads, smem) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_dyn(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
+                       uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s)
+{
+    const int smem = dyn_layout(max_block).total;
+    cudaError_t e = cudaFuncSetAttribute(k_rle_dyn_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_rle_dyn_blocks<<<grid, kDynThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    note_launch();
+    return cudaGetLastError();
 }
 
 // hash_bits: the largest table size among the launch's images (9 or 10).

@@ -35,9 +35,11 @@ namespace r2p {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 // a graph replay launches the captured kernels again
-static void note_launch_graph(bool stored, bool lz)
+static void note_launch_graph(bool stored, bool lz, bool dyn)
 {
-    g_launches.fetch_add(3u + (stored ? 1u : 0u) + (lz ? 2u : 0u), std::memory_order_relaxed);
+    // prepare, filter, finalize; stored; LZ77; dynamic; the block copy after either
+    const uint32_t n = 3u + (stored ? 1u : 0u) + (lz ? 1u : 0u) + (dyn ? 1u : 0u) + ((lz || dyn) ? 1u : 0u);
+    g_launches.fetch_add(n, std::memory_order_relaxed);
 }
 
 static thread_local std::string t_last_error;
@@ -372,7 +374,7 @@ struct Prepared {
     std::vector<BlockOut> blocks;
     int smem = 0, slots_total = 0, max_block = 0;
     uint32_t nblk = 0;
-    bool any_lz = false, any_stored = false;
+    bool any_lz = false, any_stored = false, any_dyn = false;
     uint64_t slot = 0;
     size_t o_img = 0, o_items = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0, o_extra = 0;
     size_t total = 0;
@@ -436,7 +438,9 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
         }
         P.nblk += (uint32_t)d.nblocks;
         P.max_block = std::max(P.max_block, d.block_size);
-        if (d.level == 0) P.any_stored = true; else P.any_lz = true;
+        if (d.level == 0) P.any_stored = true;
+        else if (d.level == 1) P.any_lz = true;
+        else P.any_dyn = true;
         d.hash_bits = plans[i].hash_bits == 9 ? 9 : 10;
         if (d.level > 0 && d.hash_bits == 10) any10 = true;
         lut_total += plans[i].lut_cap;
@@ -445,7 +449,7 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
     }
     // one hash-table size per launch: the one most blocks were tuned for
     P.hash_bits = any10 ? 10 : 9;      // LZ77 tables sized for the largest; each block uses its image's
-    P.slot = P.any_lz ? lz77_slot_bytes(P.max_block) : 0;
+    P.slot = (P.any_lz || P.any_dyn) ? lz77_slot_bytes(P.max_block) : 0;
     Layout L;
     P.o_img = L.take(sizeof(DevImage) * n);
     P.o_items = L.take(sizeof(BandItem) * std::max<size_t>(1, P.items.size()));
@@ -520,12 +524,17 @@ static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, in
         R2P_CU(launch_lz77(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, bgrid,
                            P.hash_bits, s),
                "k_lz77_blocks");
-    R2P_CU(mark(4, defl && P.any_lz), "event");
+    if (defl && P.any_dyn) {
+        const int dgrid = (int)std::min<uint64_t>(P.nblk, (uint64_t)e->nsm * dyn_ctas_per_sm(P.max_block));
+        R2P_CU(launch_dyn(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, dgrid, s),
+               "k_rle_dyn_blocks");                      // timed in the LZ77 slot
+    }
+    R2P_CU(mark(4, defl && (P.any_lz || P.any_dyn)), "event");
     if (defl) R2P_CU(launch_finalize(dimg, n, dblocks, e->d_xpow, s), "k_finalize");
     R2P_CU(mark(5, defl), "event");
-    if (defl && P.any_lz)
+    if (defl && (P.any_lz || P.any_dyn))
         R2P_CU(launch_copy_blocks(dimg, dblocks, (int)P.nblk, A + P.o_scratch, P.slot, bgrid, s), "k_copy_blocks");
-    R2P_CU(mark(6, defl && P.any_lz), "event");
+    R2P_CU(mark(6, defl && (P.any_lz || P.any_dyn)), "event");
     return R2P_OK;
 }
 
@@ -1265,7 +1274,7 @@ int r2p_batch_launch_graph(r2p_batch* b, void* stream)
         if (ce != cudaSuccess) return cuda_err(ce, "graph capture");
     }
     R2P_CU(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
-    note_launch_graph(b->P.any_stored, b->P.any_lz);
+    note_launch_graph(b->P.any_stored, b->P.any_lz, b->P.any_dyn);
     return R2P_OK;
 }
 
