@@ -384,50 +384,58 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
 // Filtered scanlines are mostly small residuals and runs; coding them with a
 // per-block Huffman code (RFC 1951 3.2.7) matters far more than a match
 // search (zlib's run-length strategy, distance-1 matches only, is what PNG
-// encoders use for this data).  One 256-thread CTA per block, two per SM:
-//   1. stage the block; each thread parses its sub-range (tokens: a literal,
-//      or a run of 3..258 copies of the previous byte = length, distance 1)
-//      into per-warp symbol histograms;
-//   2. one thread builds the literal/length code (lengths <= 15, r2p_huff.h),
-//      the canonical codes and the block header, and sizes the block; the
-//      block is stored instead when that is smaller;
-//   3. every thread re-parses to count its bits, a CTA scan gives each its
-//      bit offset, and a third parse writes its codes straight into the
-//      block's slot (shared atomics only for the words at stream ends);
+// encoders use for this data).  One 1024-thread CTA per block:
+//   1. stage the block; each thread parses its 68-byte chunks (tokens: a
+//      literal, or a run of 3..258 copies of the previous byte = a length at
+//      distance 1) into its warp's symbol histogram;
+//   2. the literal/length code: used symbols ranked by (count, symbol) in
+//      parallel; the pairing phase of the in-place minimum-redundancy
+//      computation on one thread, internal-node depths by pointer jumping and
+//      leaves per depth level in parallel (r2p_huff.h states both forms);
+//      counts halved and the code rebuilt while it is deeper than 15;
+//      canonical codes per symbol in parallel;
+//   3. the CTA writes the block header (cta_dyn_header) and counts each
+//      thread's code bits; a CTA scan gives each thread its bit offset, the block is
+//      stored instead when that is smaller, and a last parse writes the codes
+//      straight into the block's slot (atomics only for the words that
+//      neighbouring streams share);
 //   4. end-of-block code, the empty stored block of non-final blocks, CRC.
 // ---------------------------------------------------------------------------
-constexpr int kDynThreads = 256;
-constexpr int kDynWarps = kDynThreads / 32;
+constexpr int kDynRounds = 9;                  // pointer-jumping rounds: depths < 512
 
-// Bytes per thread: a multiple of 4 with an odd word count (distinct banks).
+// Bytes per chunk for NT chunks: a multiple of 4 with an odd word count (the
+// lanes of a warp start on distinct banks).
+template <int NT>
 __host__ __device__ inline int dyn_sub_bytes(int block_size)
 {
-    const int w = ((block_size + kDynThreads - 1) / kDynThreads + 3) >> 2;
+    const int w = ((block_size + NT - 1) / NT + 3) >> 2;
     return 4 * (w | 1);
 }
 
-struct DynLayout {
-    int in, hist, freq, wt, lt, sorted, lltab, lens, codes, hw, lsym, total;
+// Shared memory of the dynamic kernel with NT threads: fixed-size tables
+// first (compile-time offsets), the staged block last.
+template <int NT>
+struct DynSmem {
+    static constexpr int Warps = NT / 32;
+    static constexpr int Hist = 4096;                            // after the CRC tables
+    static constexpr int Freq = Hist + Warps * kLLSyms * 4;
+    static constexpr int Wt = Freq + kLLSyms * 4;
+    static constexpr int Par = Wt + kLLSyms * 4;
+    static constexpr int Dep = Par + kLLSyms * 4;
+    static constexpr int Sorted = Dep + kLLSyms * 4;
+    static constexpr int Lltab = Sorted + ((kLLSyms * 2 + 15) & ~15);
+    static constexpr int Lens = Lltab + kLLSyms * 4;
+    static constexpr int Hw = Lens + ((kLLSyms + kDSyms + 15) & ~15);
+    static constexpr int Lsym = Hw + kHdrWords * 4;
+    static constexpr int Lvl = Lsym + 256 * 4;                   // per depth: internal count, leaves so far; per length
+    static constexpr int All = Lvl + 3 * 64 * 4;                 // header: code lengths in order
+    static constexpr int Rs = All + 320;                         //   run-length symbols
+    static constexpr int Rx = Rs + 320;                          //   their extra values
+    static constexpr int Cl = Rx + 320;                          //   CL counts (19 u32), lengths, codes
+    static constexpr int In = (Cl + 19 * 4 + 32 + 48 + 15) & ~15;  // 16-byte staging stores
+    static_assert(In % 16 == 0 && Hw % 4 == 0 && Lsym % 4 == 0 && Lltab % 4 == 0 && NT >= 512, "layout");
+    static int bytes(int max_block) { return In + lz_in_bytes(max_block); }
 };
-
-__host__ __device__ inline DynLayout dyn_layout(int max_block)
-{
-    DynLayout L;
-    int o = 4096;                                   // CRC tables
-    L.in = o;     o += lz_in_bytes(max_block);
-    L.hist = o;   o += kDynWarps * kLLSyms * 4;
-    L.freq = o;   o += kLLSyms * 4;
-    L.wt = o;     o += kLLSyms * 4;
-    L.lt = o;     o += kLLSyms * 4;
-    L.sorted = o; o += ((kLLSyms * 2 + 15) & ~15);
-    L.lltab = o;  o += kLLSyms * 4;
-    L.lens = o;   o += ((kLLSyms + kDSyms + 15) & ~15);
-    L.codes = o;  o += (((kLLSyms + kDSyms) * 2 + 15) & ~15);
-    L.hw = o;     o += kHdrWords * 4;
-    L.lsym = o;   o += 256 * 4;
-    L.total = o;
-    return L;
-}
 
 // Run-length parse of in[s, e): calls f.lit(byte) or f.match(len 3..258).
 template <class F>
@@ -464,18 +472,31 @@ __device__ __forceinline__ void rle_parse(const uint8_t* in, int s, int e, F& f)
     }
 }
 
+// The block's tokens do not depend on the CTA size: it is cut into 1024
+// chunks of dyn_sub_bytes<1024> bytes (runs end at chunk ends) and thread t
+// of NT parses chunks t * (1024 / NT) onward, so its bits stay contiguous.
+template <int NT, class F>
+__device__ __forceinline__ void rle_parse_chunks(const uint8_t* in, int n, F& f)
+{
+    constexpr int kChunks = 1024 / NT;
+    const int sub = dyn_sub_bytes<1024>(n);
+#pragma unroll
+    for (int c = 0; c < kChunks; c++) {
+        const int s = min(n, ((int)threadIdx.x * kChunks + c) * sub);
+        rle_parse(in, s, min(n, s + sub), f);
+    }
+}
+
 // lsym[len - 3] = length symbol | extra bit count << 9 | extra value << 12
 struct RleHist {
     uint32_t* h;
     const uint32_t* lsym;
-    uint32_t matches, extra;
+    uint32_t matches;
     __device__ void lit(uint32_t b) { atomicAdd(&h[b], 1u); }
     __device__ void match(int L)
     {
-        const uint32_t e = lsym[L - 3];
-        atomicAdd(&h[e & 511u], 1u);
+        atomicAdd(&h[lsym[L - 3] & 511u], 1u);
         matches++;
-        extra += (e >> 9) & 7u;
     }
 };
 
@@ -552,31 +573,131 @@ __device__ __forceinline__ void or_bits_global(uint32_t* w, uint32_t pos, uint32
     if (sh + n > 32u) atomicOr(w + q + 1, v >> (32u - sh));
 }
 
-__global__ void __launch_bounds__(kDynThreads)
+// Exclusive CTA-wide prefix sum of v (and the total); all threads call it.
+template <int NT>
+__device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t* wsum, uint32_t& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0, tot = 0;
+    for (int k = 0; k < NT / 32; k++) {
+        const uint32_t w = wsum[k];
+        base += k < warp ? w : 0u;
+        tot += w;
+    }
+    __syncthreads();
+    total = tot;
+    return base + incl - v;
+}
+
+// The block's header (BFINAL, BTYPE = 10 and what build_dyn_header writes,
+// bit for bit) built by the whole CTA: the thread at the first entry of each
+// run of equal code lengths writes that run's symbols at its scanned
+// position, one thread builds the 19-symbol code-length code, and every
+// symbol then ORs its code and extra bits in at its scanned bit offset.
+// hw (kHdrWords words) is zeroed here; returns the header's end bit.
+template <int NT>
+__device__ uint32_t cta_dyn_header(const uint8_t* ll_len, const uint8_t* d_len, uint32_t* hw, bool last, uint8_t* sm,
+                                   uint32_t* wsum, uint32_t* s_hdr)
+{
+    using S = DynSmem<NT>;
+    const int tid = threadIdx.x;
+    uint8_t* all = sm + S::All;
+    uint8_t* rs = sm + S::Rs;
+    uint8_t* rx = sm + S::Rx;
+    uint32_t* cf = reinterpret_cast<uint32_t*>(sm + S::Cl);
+    uint8_t* cl_len = sm + S::Cl + 19 * 4;
+    uint16_t* cl_code = reinterpret_cast<uint16_t*>(sm + S::Cl + 19 * 4 + 32);
+    for (int k = tid; k < kHdrWords; k += NT) hw[k] = 0u;
+    if (tid < kCLSyms) cf[tid] = 0u;
+    if (tid < 2) s_hdr[tid] = 0u;
+    __syncthreads();
+    if (tid < kLLSyms && ll_len[tid]) atomicMax(&s_hdr[0], (uint32_t)tid + 1u);
+    if (tid < kDSyms && d_len[tid]) atomicMax(&s_hdr[1], (uint32_t)tid + 1u);
+    __syncthreads();
+    const int nll = max(257, (int)s_hdr[0]), nd = max(1, (int)s_hdr[1]), n = nll + nd;
+    if (tid < n) all[tid] = tid < nll ? ll_len[tid] : d_len[tid - nll];
+    __syncthreads();
+    int l = 0, run = 0;
+    uint32_t k = 0;
+    if (tid < n && (tid == 0 || all[tid] != all[tid - 1])) {
+        l = all[tid];
+        run = 1;
+        while (tid + run < n && all[tid + run] == l) run++;
+        k = (uint32_t)rle_run_count(l, run);
+    }
+    uint32_t nr;
+    const uint32_t at = cta_excl_scan<NT>(k, wsum, nr);
+    if (k) rle_run_write(l, run, rs + at, rx + at);
+    __syncthreads();
+    if (tid < (int)nr) atomicAdd(&cf[rs[tid]], 1u);
+    __syncthreads();
+    if (tid == 0) {
+        const int ncl = cl_code_build(cf, cl_len, cl_code);
+        uint32_t pos = 0;
+        put_bits(hw, pos, last ? 5u : 4u, 3);
+        put_header_counts(hw, pos, nll, nd, ncl, cl_len);
+        s_hdr[2] = pos;
+    }
+    __syncthreads();
+    uint32_t nb = 0, v = 0;
+    if (tid < (int)nr) {
+        const int sym = rs[tid];
+        nb = (uint32_t)(cl_len[sym] + cl_extra_bits(sym));
+        v = (uint32_t)cl_code[sym] | ((uint32_t)rx[tid] << cl_len[sym]);
+    }
+    uint32_t tot;
+    const uint32_t off = s_hdr[2] + cta_excl_scan<NT>(nb, wsum, tot);
+    if (nb) {
+        const uint32_t q = off >> 5, sh = off & 31u;
+        atomicOr(&hw[q], v << sh);
+        if (sh + nb > 32u) atomicOr(&hw[q + 1], v >> (32u - sh));
+    }
+    __syncthreads();
+    return s_hdr[2] + tot;
+}
+
+// NT threads: 1024 (one CTA per SM, the shortest per-block latency) for
+// launches with at most one block per SM, 512 (two CTAs per SM, one's
+// single-thread phases hidden behind the other's parses) for more; both
+// write the same bytes (rle_parse_chunks).
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT)
 k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int max_block,
                  uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
 {
+    using S = DynSmem<NT>;
+    constexpr int kDynThreads = NT, kDynWarps = NT / 32;
     extern __shared__ __align__(16) uint8_t sm[];
-    const DynLayout Ly = dyn_layout(max_block);
     uint32_t (*ctab)[256] = reinterpret_cast<uint32_t (*)[256]>(sm);
-    uint8_t* in = sm + Ly.in;
+    uint8_t* in = sm + S::In;
     const int in_bytes = lz_in_bytes(max_block);
-    uint32_t* hist = reinterpret_cast<uint32_t*>(sm + Ly.hist);
-    uint32_t* freq = reinterpret_cast<uint32_t*>(sm + Ly.freq);
-    uint32_t* wt = reinterpret_cast<uint32_t*>(sm + Ly.wt);
-    uint32_t* lt = reinterpret_cast<uint32_t*>(sm + Ly.lt);
-    uint16_t* sorted = reinterpret_cast<uint16_t*>(sm + Ly.sorted);
-    uint32_t* lltab = reinterpret_cast<uint32_t*>(sm + Ly.lltab);
-    uint8_t* ll_len = sm + Ly.lens;
+    uint32_t* hist = reinterpret_cast<uint32_t*>(sm + S::Hist);
+    uint32_t* freq = reinterpret_cast<uint32_t*>(sm + S::Freq);
+    uint32_t* P = reinterpret_cast<uint32_t*>(sm + S::Wt);       // weights, then parents (phase 1)
+    uint32_t* par = reinterpret_cast<uint32_t*>(sm + S::Par);
+    uint32_t* dep = reinterpret_cast<uint32_t*>(sm + S::Dep);
+    uint16_t* sorted = reinterpret_cast<uint16_t*>(sm + S::Sorted);
+    uint32_t* lltab = reinterpret_cast<uint32_t*>(sm + S::Lltab);
+    uint8_t* ll_len = sm + S::Lens;
     uint8_t* d_len = ll_len + kLLSyms;
-    uint16_t* ll_code = reinterpret_cast<uint16_t*>(sm + Ly.codes);
-    uint16_t* d_code = ll_code + kLLSyms;
-    uint32_t* hw = reinterpret_cast<uint32_t*>(sm + Ly.hw);
-    uint32_t* lsym = reinterpret_cast<uint32_t*>(sm + Ly.lsym);
+    uint32_t* hw = reinterpret_cast<uint32_t*>(sm + S::Hw);
+    uint32_t* lsym = reinterpret_cast<uint32_t*>(sm + S::Lsym);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(sm + S::Lvl);   // internal nodes per depth
+    uint32_t* cum = cnt + 64;                                    // leaves at depth <= d
+    uint32_t* blc = cnt + 128;                                   // codes per length, then next code
     __shared__ uint64_t red64[kDynWarps];
     __shared__ uint32_t red32[kDynWarps];
     __shared__ uint32_t wsum[kDynWarps];
     __shared__ uint32_t s_info[4];
+    __shared__ uint32_t s_hdr[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     build_crc_tables(ctab);
     for (int i = tid; i < 256; i += kDynThreads) {
@@ -592,6 +713,8 @@ k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ block
         const int n = (int)bo.in_len;
         const uint8_t* src = d.filt + bo.in_off;
         const bool last = ((int)(b - d.blk0) == d.nblocks - 1) && !d.open_end;
+        uint8_t* slot = scratch + (size_t)b * slot_bytes;
+        uint32_t* out = reinterpret_cast<uint32_t*>(slot);
         __syncthreads();
         if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
             for (int i = tid; i < (n >> 4); i += kDynThreads)
@@ -603,96 +726,146 @@ k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ block
         for (int i = n + tid; i < in_bytes; i += kDynThreads) in[i] = 0;
         for (int i = tid; i < kDynWarps * kLLSyms; i += kDynThreads) hist[i] = 0u;
         for (int i = tid; i < kLLSyms + kDSyms; i += kDynThreads) ll_len[i] = 0;
+        for (int i = tid; i < (n + kStoredHdr + 3) / 4 + 2; i += kDynThreads) out[i] = 0u;   // any dynamic size
         __syncthreads();
         uint32_t s1;
         uint64_t s2;
         cta_adler_sums<kDynThreads>(in, n, s1, s2, red64);
-        const int sub = dyn_sub_bytes(n);
-        const int s = min(n, tid * sub), e = min(n, s + sub);
         // 1. histogram
-        RleHist H{hist + warp * kLLSyms, lsym, 0u, 0u};
-        rle_parse(in, s, e, H);
+        RleHist H{hist + warp * kLLSyms, lsym, 0u};
+        rle_parse_chunks<NT>(in, n, H);
         const uint32_t matches = (uint32_t)cta_sum64<kDynThreads>(H.matches, red64);
-        const uint64_t extra = cta_sum64<kDynThreads>(H.extra, red64);
-        for (int i = tid; i < kLLSyms; i += kDynThreads) {
-            uint32_t f = (i == 256) ? 1u : 0u;        // one end-of-block code
-            for (int w = 0; w < kDynWarps; w++) f += hist[w * kLLSyms + i];
-            freq[i] = f;
+        uint32_t f = 0;
+        if (tid < kLLSyms) {
+            f = (tid == 256) ? 1u : 0u;                  // one end-of-block code
+            for (int w = 0; w < kDynWarps; w++) f += hist[w * kLLSyms + tid];
+            freq[tid] = f;
         }
-        __syncthreads();
-        // 2. used symbols sorted by (frequency, symbol): each thread ranks its own
-        for (int i = tid; i < kLLSyms; i += kDynThreads) {
-            const uint32_t f = freq[i];
-            if (!f) continue;
+        const int nu = __syncthreads_count(f != 0u);
+        // 2. used symbols sorted by (count, symbol)
+        if (f) {
             int r = 0;
+#pragma unroll 8
             for (int j = 0; j < kLLSyms; j++) {
                 const uint32_t g = freq[j];
-                r += (g && (g < f || (g == f && j < i))) ? 1 : 0;
+                r += (g != 0u && (g < f || (g == f && j < tid))) ? 1 : 0;
             }
-            sorted[r] = (uint16_t)i;
+            sorted[r] = (uint16_t)tid;
         }
         __syncthreads();
-        if (tid == 0) {
-            int nu = 0;
-            for (int i = 0; i < kLLSyms; i++) nu += freq[i] ? 1 : 0;
-            for (int i = 0; i < nu; i++) wt[i] = freq[sorted[i]];
-            if (nu >= 2) limited_lengths(wt, nu, kMaxCodeLen, lt);
-            else lt[0] = 1;                            // (a block always has a literal and the end code)
-            s_info[3] = (uint32_t)nu;
+        const int root = nu - 2;                        // nu >= 2: a literal and the end code
+        for (uint32_t sh = 0;; sh++) {
+            if (tid < nu) P[tid] = (uint32_t)(((uint64_t)freq[sorted[tid]] + (1u << sh) - 1u) >> sh);
+            if (tid < 64) cnt[tid] = 0u;
+            __syncthreads();
+            if (tid == 0) mk_phase1(P, nu);
+            __syncthreads();
+            // depths of the internal nodes 0..nu-2 by pointer jumping
+            if (tid <= root) {
+                par[tid] = tid == root ? (uint32_t)root : P[tid];
+                dep[tid] = tid == root ? 0u : 1u;
+            }
+            __syncthreads();
+            for (int r = 0; r < kDynRounds; r++) {
+                uint32_t nd = 0, np = 0;
+                if (tid <= root) {
+                    const uint32_t pk = par[tid];
+                    nd = dep[tid] + dep[pk];
+                    np = par[pk];
+                }
+                __syncthreads();
+                if (tid <= root) {
+                    dep[tid] = nd;
+                    par[tid] = np;
+                }
+                __syncthreads();
+            }
+            if (tid <= root) atomicAdd(&cnt[min(dep[tid], 63u)], 1u);   // depths stay below 24 for 64 KB blocks
+            __syncthreads();
+            if (tid == 0) {                              // leaves per depth level, from the top
+                uint32_t places = 1, leaves = 0;
+                int dmax = 0;
+                for (int dd = 0; dd < 64; dd++) {
+                    const uint32_t lv = places - cnt[dd];
+                    leaves += lv;
+                    cum[dd] = leaves;
+                    if (lv) dmax = dd;
+                    places = 2 * cnt[dd];
+                }
+                s_info[3] = (uint32_t)dmax;
+            }
+            __syncthreads();
+            if ((int)s_info[3] <= kMaxCodeLen) break;
+            __syncthreads();
         }
+        // leaf tid (ascending count) takes the depth whose range holds it
+        if (tid < nu) {
+            const uint32_t from_top = (uint32_t)(nu - tid);
+            int dd = 1;
+            while (cum[dd] < from_top) dd++;
+            ll_len[sorted[tid]] = (uint8_t)dd;
+        }
+        if (tid < 16) blc[tid] = 0u;
         __syncthreads();
-        const int nu = (int)s_info[3];
-        for (int i = tid; i < nu; i += kDynThreads) ll_len[sorted[i]] = (uint8_t)lt[i];
+        // 3. canonical codes; the header (one thread) while the rest count bits
+        const int myl = tid < kLLSyms ? ll_len[tid] : 0;
+        if (myl) atomicAdd(&blc[myl], 1u);
         __syncthreads();
         if (tid == 0) {
+            uint32_t c = 0;
+            for (int l = 1; l <= kMaxCodeLen; l++) {
+                c = (c + (l > 1 ? blc[l - 1] : 0u)) << 1;
+                blc[16 + l] = c;                         // first code of length l
+            }
             d_len[0] = matches ? 1 : 0;
-            canonical_codes(ll_len, kLLSyms, ll_code);
-            canonical_codes(d_len, kDSyms, d_code);
-            for (int k = 0; k < kHdrWords; k++) hw[k] = 0u;
-            uint32_t pos = 0;
-            put_bits(hw, pos, last ? 5u : 4u, 3);      // BFINAL, BTYPE = 10
-            const uint32_t hend = build_dyn_header(ll_len, d_len, hw, pos);
-            uint64_t body = 0;
-            for (int i = 0; i < kLLSyms; i++) body += (uint64_t)freq[i] * ll_len[i];
-            const uint64_t total = hend + body + extra + (uint64_t)matches * d_len[0];
-            const uint64_t dyn = last ? (total + 7) / 8 : (total + 3 + 7) / 8 + 4;
-            s_info[0] = (dyn < (uint64_t)(n + kStoredHdr)) ? (uint32_t)dyn : 0u;   // 0 = stored block
-            s_info[1] = hend;
-            s_info[2] = (uint32_t)total;
         }
         __syncthreads();
-        for (int i = tid; i < kLLSyms; i += kDynThreads) lltab[i] = (uint32_t)ll_code[i] | ((uint32_t)ll_len[i] << 16);
+        if (tid < kLLSyms) {
+            uint32_t code = 0;
+            if (myl) {
+                uint32_t r = 0;
+#pragma unroll 8
+                for (int j = 0; j < kLLSyms; j++) r += (j < tid && ll_len[j] == myl) ? 1u : 0u;
+                code = bitrev(blc[16 + myl] + r, myl);
+            }
+            lltab[tid] = code | ((uint32_t)myl << 16);
+        }
+        __syncthreads();
+        const uint32_t hend = cta_dyn_header<NT>(ll_len, d_len, hw, last, sm, wsum, s_hdr);
+        RleCount C{lltab, lsym, (uint32_t)d_len[0], 0u};
+        rle_parse_chunks<NT>(in, n, C);
+        uint32_t incl = C.bits;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t body = 0;
+            for (int k = 0; k < kDynWarps; k++) body += wsum[k];
+            const uint32_t total = hend + body + (lltab[256] >> 16);
+            const uint32_t dyn = last ? (total + 7) / 8 : (total + 3 + 7) / 8 + 4;
+            s_info[0] = (dyn < (uint32_t)(n + kStoredHdr)) ? dyn : 0u;    // 0 = stored block
+            s_info[2] = total;
+            if (s_info[0])
+                for (int k = 0; k < (int)((hend + 31) / 32); k++) out[k] = hw[k];
+        }
+        __syncthreads();
         const uint32_t dyn = s_info[0];
-        uint8_t* slot = scratch + (size_t)b * slot_bytes;
         uint32_t crc;
         if (dyn) {
-            const uint32_t hend = s_info[1], total = s_info[2];
-            uint32_t* out = reinterpret_cast<uint32_t*>(slot);
-            const int owords = (int)((dyn + 3) / 4) + 1;
-            for (int i = tid; i < owords; i += kDynThreads) out[i] = 0u;
-            __syncthreads();
-            // 3. bit counts, offsets, codes
-            RleCount C{lltab, lsym, (uint32_t)d_len[0], 0u};
-            rle_parse(in, s, e, C);
-            uint32_t incl = C.bits;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += y;
-            }
-            if (lane == 31) wsum[warp] = incl;
-            if (tid == 0)
-                for (int k = 0; k < (int)((hend + 31) / 32); k++) out[k] = hw[k];
-            __syncthreads();
+            const uint32_t total = s_info[2];
             uint32_t wbase = 0;
             for (int k = 0; k < warp; k++) wbase += wsum[k];
             RleEmit E;
             E.tab = lltab;
             E.lsym = lsym;
-            E.dcode = d_code[0];
+            E.dcode = 0;                                 // the one distance code, length 1
             E.dlen = d_len[0];
             E.init(out, hend + wbase + incl - C.bits);
-            rle_parse(in, s, e, E);
+            rle_parse_chunks<NT>(in, n, E);
             E.finish();
             __syncthreads();
             if (tid == 0) {
@@ -727,24 +900,33 @@ k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ block
     }
 }
 
-int dyn_ctas_per_sm(int max_block)
+// Threads per CTA for a launch of nblocks blocks on nsm SMs (1024 while the
+// blocks fit one CTA per SM, else 512 with two CTAs per SM) and its grid.
+int dyn_grid(int nblocks, int nsm, int* threads)
 {
-    int n = 0;
-    const int smem = dyn_layout(max_block).total;
-    cudaFuncSetAttribute(k_rle_dyn_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rle_dyn_blocks, kDynThreads, smem) != cudaSuccess) return 1;
-    return n > 0 ? n : 1;
+    *threads = nblocks <= nsm ? 1024 : 512;
+    return std::max(1, std::min(nblocks, *threads == 1024 ? nsm : 2 * nsm));
+}
+
+template <int NT>
+static cudaError_t launch_dyn_t(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
+                                uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s)
+{
+    const int smem = DynSmem<NT>::bytes(max_block);
+    cudaError_t e = cudaFuncSetAttribute(k_rle_dyn_blocks<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_rle_dyn_blocks<NT><<<grid, NT, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    note_launch();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_dyn(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
-                       uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s)
+                       uint64_t slot_bytes, const uint32_t* xpow, int nsm, cudaStream_t s)
 {
-    const int smem = dyn_layout(max_block).total;
-    cudaError_t e = cudaFuncSetAttribute(k_rle_dyn_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    k_rle_dyn_blocks<<<grid, kDynThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
-    note_launch();
-    return cudaGetLastError();
+    int nt;
+    const int grid = dyn_grid(nblocks, nsm, &nt);
+    return nt == 1024 ? launch_dyn_t<1024>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow, grid, s)
+                      : launch_dyn_t<512>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow, grid, s);
 }
 
 // hash_bits: the largest table size among the launch's images (9 or 10).

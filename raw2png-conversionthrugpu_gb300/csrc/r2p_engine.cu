@@ -524,11 +524,9 @@ static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, in
         R2P_CU(launch_lz77(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, bgrid,
                            P.hash_bits, s),
                "k_lz77_blocks");
-    if (defl && P.any_dyn) {
-        const int dgrid = (int)std::min<uint64_t>(P.nblk, (uint64_t)e->nsm * dyn_ctas_per_sm(P.max_block));
-        R2P_CU(launch_dyn(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, dgrid, s),
+    if (defl && P.any_dyn)
+        R2P_CU(launch_dyn(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, e->nsm, s),
                "k_rle_dyn_blocks");                      // timed in the LZ77 slot
-    }
     R2P_CU(mark(4, defl && (P.any_lz || P.any_dyn)), "event");
     if (defl) R2P_CU(launch_finalize(dimg, n, dblocks, e->d_xpow, s), "k_finalize");
     R2P_CU(mark(5, defl), "event");

@@ -20,12 +20,14 @@ constexpr int kHdrWords = 144;
 
 // Minimum-redundancy code lengths computed in place, after Moffat and
 // Katajainen, "In-place calculation of minimum-redundancy codes" (WADS 1995).
-// A[0..n-1] holds n >= 2 weights in non-decreasing order; on return A[i] is
-// the code length of the i-th weight (so lengths are non-increasing in i).
-R2P_HD void mk_lengths_inplace(uint32_t* A, int n)
+// A[0..n-1] holds n >= 2 weights in non-decreasing order.
+//
+// Phase 1 pairs the two smallest items repeatedly.  Internal node k (k = 0
+// .. n-2, created in order of non-decreasing weight) keeps its weight in A[k]
+// until it is paired, then the index of its parent; the root n-2 keeps the
+// total weight.
+R2P_HD void mk_phase1(uint32_t* A, int n)
 {
-    // 1. pair the two smallest items repeatedly; internal nodes keep their
-    //    weight until they are paired, then the index of their parent
     A[0] += A[1];
     int root = 0, leaf = 2;
     for (int next = 1; next < n - 1; next++) {
@@ -42,13 +44,39 @@ R2P_HD void mk_lengths_inplace(uint32_t* A, int n)
             A[next] += A[leaf++];
         }
     }
-    // 2. depth of every internal node from its parent's
+}
+
+// Phases 2 and 3 restated per depth level (the GPU runs them in parallel):
+// with c[d] internal nodes at depth d, level d offers 2 * c[d-1] places (one
+// at the root level), of which the leaves take lv[d] = places - c[d]; leaves
+// fill levels from the top, largest weight (index n-1) first.  P holds
+// phase 1's output; L receives the code length of each sorted weight, D is
+// scratch for the n-1 internal depths.  Returns the largest length.
+R2P_HD int mk_levels(const uint32_t* P, int n, uint32_t* D, uint32_t* L)
+{
+    D[n - 2] = 0;
+    for (int k = n - 3; k >= 0; k--) D[k] = D[P[k]] + 1;     // a parent's index exceeds its child's
+    uint32_t c[64];
+    for (int d = 0; d < 64; d++) c[d] = 0;
+    for (int k = 0; k < n - 1; k++) c[D[k]]++;
+    int idx = n - 1, d = 0;
+    uint32_t places = 1;
+    for (; idx >= 0; d++) {
+        const uint32_t lv = places - c[d];
+        for (uint32_t k = 0; k < lv; k++) L[idx--] = (uint32_t)d;
+        places = 2 * c[d];
+    }
+    return d - 1;
+}
+
+// The whole computation in place (phases 2-3 as the published sequential
+// loops): on return A[i] is the code length of the i-th weight.
+R2P_HD void mk_lengths_inplace(uint32_t* A, int n)
+{
+    mk_phase1(A, n);
     A[n - 2] = 0;
     for (int next = n - 3; next >= 0; next--) A[next] = A[A[next]] + 1;
-    // 3. leaves per depth: each level offers twice the internal nodes of the
-    //    level above; what internal nodes do not take is leaves
-    int avail = 1, used = 0, depth = 0, next = n - 1;
-    root = n - 2;
+    int avail = 1, used = 0, depth = 0, next = n - 1, root = n - 2;
     while (avail > 0) {
         while (root >= 0 && (int)A[root] == depth) {
             used++;
@@ -139,6 +167,90 @@ R2P_HD void put_bits(uint32_t* w, uint32_t& pos, uint32_t v, int n)
     pos += (uint32_t)n;
 }
 
+// Run-length symbols for one run of `run` equal code lengths l (RFC 1951
+// 3.2.7): zeros as 18 (11-138) and 17 (3-10), other lengths once and then 16
+// (repeat 3-6); what is left over is written out.  rle_run_count gives the
+// number of symbols, rle_run_write writes them (symbol, extra value).
+R2P_HD int rle_run_count(int l, int run)
+{
+    int r = run, k = 0;
+    if (l == 0) {
+        for (; r >= 11; k++) r -= r < 138 ? r : 138;
+        if (r >= 3) {
+            k++;
+            r = 0;
+        }
+    } else {
+        k = 1;
+        for (r--; r >= 3; k++) r -= r < 6 ? r : 6;
+    }
+    return k + r;
+}
+
+R2P_HD void rle_run_write(int l, int run, uint8_t* rs, uint8_t* rx)
+{
+    int r = run, k = 0;
+    if (l == 0) {
+        while (r >= 11) {
+            const int t = r < 138 ? r : 138;
+            rs[k] = 18;
+            rx[k++] = (uint8_t)(t - 11);
+            r -= t;
+        }
+        if (r >= 3) {
+            rs[k] = 17;
+            rx[k++] = (uint8_t)(r - 3);
+            r = 0;
+        }
+    } else {
+        rs[k] = (uint8_t)l;
+        rx[k++] = 0;
+        r--;
+        while (r >= 3) {
+            const int t = r < 6 ? r : 6;
+            rs[k] = 16;
+            rx[k++] = (uint8_t)(t - 3);
+            r -= t;
+        }
+    }
+    while (r > 0) {
+        rs[k] = (uint8_t)l;
+        rx[k++] = 0;
+        r--;
+    }
+}
+
+// Extra bits after a code-length symbol.
+R2P_HD int cl_extra_bits(int sym) { return sym == 16 ? 2 : sym == 17 ? 3 : sym == 18 ? 7 : 0; }
+
+// The code-length code (lengths <= 7; a lone symbol is completed by an unused
+// one, as inflate wants a complete code here) and HCLEN's count: the
+// permuted positions up to the last used, at least 4.
+R2P_HD int cl_code_build(const uint32_t* cf, uint8_t* cl_len, uint16_t* cl_code)
+{
+    uint16_t sym[kCLSyms];
+    uint32_t wt[kCLSyms], lt[kCLSyms];
+    for (int s = 0; s < kCLSyms; s++) cl_len[s] = 0;
+    const int nu = sort_used(cf, kCLSyms, sym);
+    lengths_from_sorted(cf, sym, nu, kMaxCLLen, cl_len, wt, lt);
+    if (nu == 1) cl_len[sym[0] == 0 ? 1 : 0] = 1;
+    canonical_codes(cl_len, kCLSyms, cl_code);
+    const uint8_t ord[kCLSyms] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+    int ncl = kCLSyms;
+    while (ncl > 4 && cl_len[ord[ncl - 1]] == 0) ncl--;
+    return ncl;
+}
+
+// HLIT, HDIST, HCLEN and the HCLEN code-length-code lengths, from bit pos.
+R2P_HD void put_header_counts(uint32_t* hw, uint32_t& pos, int nll, int nd, int ncl, const uint8_t* cl_len)
+{
+    const uint8_t ord[kCLSyms] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+    put_bits(hw, pos, (uint32_t)(nll - 257), 5);
+    put_bits(hw, pos, (uint32_t)(nd - 1), 5);
+    put_bits(hw, pos, (uint32_t)(ncl - 4), 4);
+    for (int k = 0; k < ncl; k++) put_bits(hw, pos, cl_len[ord[k]], 3);
+}
+
 // Dynamic block header after the 3 block-type bits: HLIT, HDIST, HCLEN, the
 // code-length code's lengths (in the RFC's permuted order), then both
 // alphabets' code lengths as one run-length coded sequence (16: repeat the
@@ -158,62 +270,23 @@ R2P_HD uint32_t build_dyn_header(const uint8_t* ll_len, const uint8_t* d_len, ui
         const uint8_t l = i < nll ? ll_len[i] : d_len[i - nll];
         int run = 1;
         while (i + run < n && (i + run < nll ? ll_len[i + run] : d_len[i + run - nll]) == l) run++;
-        int r = run;
-        if (l == 0) {
-            while (r >= 11) {
-                const int t = r < 138 ? r : 138;
-                rs[nr] = 18;
-                rx[nr++] = (uint8_t)(t - 11);
-                r -= t;
-            }
-            if (r >= 3) {
-                rs[nr] = 17;
-                rx[nr++] = (uint8_t)(r - 3);
-                r = 0;
-            }
-        } else {
-            rs[nr] = l;
-            rx[nr++] = 0;
-            r--;
-            while (r >= 3) {
-                const int t = r < 6 ? r : 6;
-                rs[nr] = 16;
-                rx[nr++] = (uint8_t)(t - 3);
-                r -= t;
-            }
-        }
-        while (r > 0) {
-            rs[nr] = l;
-            rx[nr++] = 0;
-            r--;
-        }
+        rle_run_write(l, run, rs + nr, rx + nr);
+        nr += rle_run_count(l, run);
         i += run;
     }
     uint32_t cf[kCLSyms];
     for (int s = 0; s < kCLSyms; s++) cf[s] = 0;
     for (int j = 0; j < nr; j++) cf[rs[j]]++;
-    uint16_t sym[kCLSyms], cl_code[kCLSyms];
-    uint32_t wt[kCLSyms], lt[kCLSyms];
     uint8_t cl_len[kCLSyms];
-    for (int s = 0; s < kCLSyms; s++) cl_len[s] = 0;
-    const int nu = sort_used(cf, kCLSyms, sym);
-    lengths_from_sorted(cf, sym, nu, kMaxCLLen, cl_len, wt, lt);
-    if (nu == 1) cl_len[sym[0] == 0 ? 1 : 0] = 1;    // a lone code is completed by an unused one
-    canonical_codes(cl_len, kCLSyms, cl_code);
-    const uint8_t ord[kCLSyms] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
-    int ncl = kCLSyms;
-    while (ncl > 4 && cl_len[ord[ncl - 1]] == 0) ncl--;
+    uint16_t cl_code[kCLSyms];
+    const int ncl = cl_code_build(cf, cl_len, cl_code);
     uint32_t pos = pos0;
-    put_bits(hw, pos, (uint32_t)(nll - 257), 5);
-    put_bits(hw, pos, (uint32_t)(nd - 1), 5);
-    put_bits(hw, pos, (uint32_t)(ncl - 4), 4);
-    for (int k = 0; k < ncl; k++) put_bits(hw, pos, cl_len[ord[k]], 3);
+    put_header_counts(hw, pos, nll, nd, ncl, cl_len);
     for (int j = 0; j < nr; j++) {
         const int s = rs[j];
         put_bits(hw, pos, cl_code[s], cl_len[s]);
-        if (s == 16) put_bits(hw, pos, rx[j], 2);
-        else if (s == 17) put_bits(hw, pos, rx[j], 3);
-        else if (s == 18) put_bits(hw, pos, rx[j], 7);
+        const int ne = cl_extra_bits(s);
+        if (ne) put_bits(hw, pos, rx[j], ne);
     }
     return pos;
 }

@@ -35,9 +35,9 @@ cudaError_t launch_checksum(const uint8_t* data, uint64_t len, bool adler, uint3
 uint64_t lz77_slot_bytes(int block_size);
 cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
                         uint64_t slot_bytes, const uint32_t* xpow, int grid, int hash_bits, cudaStream_t s);
-// levels 2-9: dynamic-Huffman blocks over a run-length parse (same slots as LZ77)
+// levels 2-9: dynamic-Huffman blocks over a run-length parse (same slots as
+// LZ77); picks its CTA size and grid from the block count and SM count
 cudaError_t launch_dyn(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
-                       uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s);
-int dyn_ctas_per_sm(int max_block);
+                       uint64_t slot_bytes, const uint32_t* xpow, int nsm, cudaStream_t s);
 
 }  // namespace r2p

@@ -181,7 +181,7 @@ extern "C" int r2p_zlib_compress_noalloc(const void* d_in, size_t len, int level
     const int grid = (int)std::min<size_t>(nb, (size_t)nd.nsm * 8);
     if (level == 0) e = launch_stored(dimg, dblk, (int)nb, bs, xpow, grid, s);
     else if (level == 1) e = launch_lz77(dimg, dblk, (int)nb, bs, slots, slot, xpow, grid, 10, s);
-    else e = launch_dyn(dimg, dblk, (int)nb, bs, slots, slot, xpow, grid, s);
+    else e = launch_dyn(dimg, dblk, (int)nb, bs, slots, slot, xpow, nd.nsm, s);
     if (e != cudaSuccess) return na_fail(e, "DEFLATE blocks");
     e = launch_finalize(dimg, 1, dblk, xpow, s);
     if (e != cudaSuccess) return na_fail(e, "k_finalize");

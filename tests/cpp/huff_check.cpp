@@ -81,6 +81,21 @@ int main(int argc, char** argv)
             while (is >> v) f.push_back((uint32_t)v);
             std::vector<uint8_t> len(f.size());
             lengths_for(f.data(), (int)f.size(), kMaxCodeLen, len.data());
+            // the per-level form of phases 2-3 gives the same lengths as the loops
+            std::vector<uint16_t> sym(f.size());
+            const int nu = sort_used(f.data(), (int)f.size(), sym.data());
+            if (nu >= 2) {
+                std::vector<uint32_t> a(nu), b(nu), P(nu), D(nu), L(nu);
+                for (int i = 0; i < nu; i++) a[i] = P[i] = f[sym[i]];
+                mk_lengths_inplace(a.data(), nu);
+                mk_phase1(P.data(), nu);
+                mk_levels(P.data(), nu, D.data(), L.data());
+                for (int i = 0; i < nu; i++)
+                    if (L[i] != a[i]) {
+                        std::printf("LEVELS-MISMATCH\n");
+                        return 1;
+                    }
+            }
             for (size_t i = 0; i < len.size(); i++) std::printf(i ? " %d" : "%d", len[i]);
             std::printf("\n");
         }

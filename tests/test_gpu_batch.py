@@ -88,3 +88,15 @@ def test_mixed_tuning_classes_same_as_alone(O, r2p, W):
         assert pngs[i] == eng.encode_png(imgs[i], raws[i]), "image %d differs between batch and alone" % i
         decode_and_check(O, r2p, imgs[i], raws[i], pngs[i])
     eng.close()
+
+
+def test_dynamic_level_batch_equals_alone(engine, O, r2p, W):
+    # a few blocks alone run the dynamic kernel with 1024-thread CTAs; a batch
+    # of many blocks runs it with 512-thread CTAs: the files must not differ
+    specs = SPECS + [(3072, 2048, 40.0, 400.0), (2048, 2500, -100.0, 700.0)]
+    imgs, raws, bufs, outs, caps, lens = make_batch_inputs(r2p, W, specs, level=6)
+    engine.encode_batch_device(imgs, [x.ptr for x in bufs], [o.ptr for o in outs], caps, lens.ptr)
+    batched = read_all(outs, lens, len(imgs))
+    for i in range(len(imgs)):
+        decode_and_check(O, r2p, imgs[i], raws[i], batched[i])
+        assert engine.encode_png(imgs[i], raws[i]) == batched[i], specs[i]
