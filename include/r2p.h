@@ -59,8 +59,12 @@ typedef struct r2p_dicom_params {
     float window_width;
 } r2p_dicom_params;
 
-/* One image to encode.  level 0 = stored DEFLATE blocks; 1..9 = LZ77 with the
- * fixed Huffman code in independent blocks (the zlib header's FLEVEL bits
+/* One image to encode.  level 0 = stored DEFLATE blocks; 1 = LZ77 with the
+ * fixed Huffman code (the reference GPU encoder's format,
+ * src/gpu_deflate_backend.cu:557-697); 2..9 = a per-block dynamic Huffman
+ * code over a run-length parse (distance-1 matches, the strategy PNG
+ * encoders use for filtered scanlines), smaller output at a lower rate.
+ * Blocks are independent at every level (the zlib header's FLEVEL bits
  * follow the level exactly as src/parallel_deflate.cpp:214-228 sets them).
  * strip_height keeps the CLI's meaning for the strip-wise entry points; the
  * whole-image entry points hold the image resident and ignore it. */
@@ -324,7 +328,7 @@ int  r2p_stream_wait_event(void* stream, void* ev);   /* later work on stream wa
 #define R2P_STAGE_PREPARE  0   /* k_prepare_window: window tables */
 #define R2P_STAGE_FILTER   1   /* k_window_filter: window + adaptive filter */
 #define R2P_STAGE_STORED   2   /* k_stored_blocks: level-0 DEFLATE */
-#define R2P_STAGE_LZ77     3   /* k_lz77_blocks: LZ77 + fixed Huffman */
+#define R2P_STAGE_LZ77     3   /* k_lz77_blocks (level 1) and k_rle_dyn_blocks (2..9) */
 #define R2P_STAGE_FINALIZE 4   /* k_finalize: checksums + PNG chunks */
 #define R2P_STAGE_COPY     5   /* k_copy_blocks: block gather */
 #define R2P_STAGE_COUNT    6
