@@ -1,4 +1,6 @@
-// k_lz77.cu -- LZ77 + fixed-Huffman DEFLATE on independent blocks.
+// k_lz77.cu -- DEFLATE on independent blocks: LZ77 + fixed Huffman (level 1,
+// k_lz77_blocks) and dynamic Huffman over a run-length parse (levels 2-9,
+// k_rle_dyn_blocks, further down).
 //
 // Reference semantics (what a block must decode to, not how it is found):
 //   fixed Huffman code + length/distance tables   src/gpu_deflate_backend.cu:76-175
