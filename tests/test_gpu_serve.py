@@ -17,18 +17,20 @@ from test_gpu_png import decode_and_check
 pytestmark = pytest.mark.gpu
 
 
-def requests(r2p, W, n, seed, cap=640):
+def requests(r2p, W, n, seed, cap=640, levels=(1,)):
     out = []
-    for (w, h, eight, wc, ww, sd) in W.request_specs(n, seed):
+    for i, (w, h, eight, wc, ww, sd) in enumerate(W.request_specs(n, seed)):
         w, h = min(w, cap), min(h, cap)
         raw = W.ct_phantom(sd, w, h)
-        img = W.image_ct8(w, h, wc, ww, level=1) if eight else W.image_ct16(w, h, wc, ww, level=1)
+        lv = levels[i % len(levels)]
+        img = W.image_ct8(w, h, wc, ww, level=lv) if eight else W.image_ct16(w, h, wc, ww, level=lv)
         out.append((img, raw))
     return out
 
 
-def test_results_same_alone_and_in_the_mix(engine, O, r2p, W):
-    items = requests(r2p, W, 48, seed=11)
+@pytest.mark.parametrize("levels", [(1,), (0, 1, 6, 9)])
+def test_results_same_alone_and_in_the_mix(engine, O, r2p, W, levels):
+    items = requests(r2p, W, 48, seed=11, cap=640 if levels == (1,) else 2048, levels=levels)
     tickets = [None] * len(items)
     with r2p.Server(0, hbm_budget=1 << 30, host_pool_bytes=256 << 20, max_inflight_batches=3) as sv:
         def client(k):
