@@ -744,16 +744,25 @@ k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ block
             freq[tid] = f;
         }
         const int nu = __syncthreads_count(f != 0u);
-        // 2. used symbols sorted by (count, symbol)
-        if (f) {
-            int r = 0;
-#pragma unroll 8
-            for (int j = 0; j < kLLSyms; j++) {
-                const uint32_t g = freq[j];
-                r += (g != 0u && (g < f || (g == f && j < tid))) ? 1 : 0;
+        // 2. used symbols sorted by (count, symbol): bitonic sort of 512 keys
+        //    count << 9 | symbol (unused symbols sort last) in the free histograms
+        uint32_t* keys = hist;
+        if (tid < 512) keys[tid] = (tid < kLLSyms && f) ? ((f << 9) | (uint32_t)tid) : 0xFFFFFFFFu;
+        __syncthreads();
+        for (int k = 2; k <= 512; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                if (tid < 256) {
+                    const int i = 2 * tid - (tid & (j - 1)), ix = i + j;
+                    const uint32_t a = keys[i], c = keys[ix];
+                    if ((a > c) == ((i & k) == 0)) {
+                        keys[i] = c;
+                        keys[ix] = a;
+                    }
+                }
+                __syncthreads();
             }
-            sorted[r] = (uint16_t)tid;
         }
+        if (tid < nu) sorted[tid] = (uint16_t)(keys[tid] & 511u);
         __syncthreads();
         const int root = nu - 2;                        // nu >= 2: a literal and the end code
         for (uint32_t sh = 0;; sh++) {
@@ -822,12 +831,24 @@ k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ block
             d_len[0] = matches ? 1 : 0;
         }
         __syncthreads();
+        // a symbol's rank among the earlier symbols of its length: ballots per
+        // length within the warp, per-warp counts for the warps before
+        constexpr int kSymWarps = (kLLSyms + 31) / 32;
+        uint32_t rank_in_warp = 0;
+        if (warp < kSymWarps) {
+            const uint32_t lt_mask = (1u << lane) - 1u;
+            for (int l = 1; l <= kMaxCodeLen; l++) {
+                const uint32_t bl = __ballot_sync(FULL, myl == l);
+                if (myl == l) rank_in_warp = __popc(bl & lt_mask);
+                if (lane == 0) dep[warp * 16 + l] = __popc(bl);     // (9 x 16 <= kLLSyms entries, free now)
+            }
+        }
+        __syncthreads();
         if (tid < kLLSyms) {
             uint32_t code = 0;
             if (myl) {
-                uint32_t r = 0;
-#pragma unroll 8
-                for (int j = 0; j < kLLSyms; j++) r += (j < tid && ll_len[j] == myl) ? 1u : 0u;
+                uint32_t r = rank_in_warp;
+                for (int w = 0; w < warp; w++) r += dep[w * 16 + myl];
                 code = bitrev(blc[16 + myl] + r, myl);
             }
             lltab[tid] = code | ((uint32_t)myl << 16);
@@ -880,9 +901,13 @@ k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ block
                 }
             }
             __syncthreads();
+            // the staged block is no longer needed: CRC the slot from a shared copy
+            for (int i = tid; i < (int)((dyn + 15) / 16); i += kDynThreads)
+                reinterpret_cast<uint4*>(in)[i] = reinterpret_cast<const uint4*>(slot)[i];
+            __syncthreads();
             uint32_t s1d;
             uint64_t s2d;
-            cta_crc_adler<kDynThreads>(slot, (int)dyn, false, ctab, xpow, crc, s1d, s2d, red64, red32);
+            cta_crc_adler<kDynThreads>(in, (int)dyn, false, ctab, xpow, crc, s1d, s2d, red64, red32);
         } else {
             uint8_t hdr[kStoredHdr] = {(uint8_t)(last ? 1 : 0), (uint8_t)(n & 0xFF), (uint8_t)(n >> 8),
                                        (uint8_t)(~n & 0xFF), (uint8_t)((~n >> 8) & 0xFF)};
