@@ -681,7 +681,7 @@ def main():
     ap.add_argument("--e2e-threads", type=int, default=6)
     ap.add_argument("--e2e-api", default="many", choices=["many", "threads"])
     ap.add_argument("--streams", type=int, default=8)
-    ap.add_argument("--server-slots", type=int, default=4)
+    ap.add_argument("--server-slots", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
