@@ -294,6 +294,15 @@ int  r2p_server_reset_stats(r2p_server* srv);
 /* Drains in-flight work, then frees everything. */
 void r2p_server_destroy(r2p_server* srv);
 
+/* ---- diagnostics ------------------------------------------------------- */
+/* Runs, on `device`, the time-bounded barrier wait that the TMA-staged
+ * kernels use for their bulk copies, on a barrier that nothing completes
+ * (arrive = 0) or that one arrival completes (arrive = 1).  *status receives
+ * what the kernel reported: R2P_ETIMEOUT once limit_us (1..1000000) has
+ * passed without completion, R2P_OK otherwise; the context stays usable.
+ * No counterpart in the reference, whose waits have no limit. */
+int r2p_selftest_bounded_wait(int device, int arrive, uint32_t limit_us, int* status);
+
 /* ---- checksums (device data) ------------------------------------------- */
 /* Replace gpu_adler32_compute (include/gpu_adler32.h:25) and
  * gpu_crc32_compute (include/gpu_crc32.h:29); results land in *d_result (a

@@ -156,6 +156,8 @@ SIGNATURES = {
     "r2p_window_filter_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp]),
     "r2p_window_filter_device_ex": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _vp, _vp, _vp]),
     "r2p_bmp_bound": (_sz, [ctypes.POINTER(Image)]),
+    "r2p_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
+                                                 ctypes.POINTER(ctypes.c_int)]),
     "r2p_encode_bmp": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _sz, ctypes.POINTER(_sz)]),
     "r2p_encode_bmp_device": (ctypes.c_int, [_vp, ctypes.POINTER(Image), _vp, _vp, _sz, _vp]),
     "r2p_zlib_compress_device": (ctypes.c_int, [_vp, _vp, _sz, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _vp]),
@@ -231,6 +233,13 @@ def check(status):
 
 def png_bound(img):
     return lib().r2p_png_bound(ctypes.byref(img))
+
+
+def selftest_bounded_wait(arrive, limit_us, device=0):
+    """Status the bounded device wait reports (r2p_selftest_bounded_wait)."""
+    st = ctypes.c_int()
+    check(lib().r2p_selftest_bounded_wait(device, 1 if arrive else 0, limit_us, ctypes.byref(st)))
+    return st.value
 
 
 def bmp_bound(img):

@@ -987,6 +987,29 @@ cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// The time-bounded barrier wait of the TMA-staged kernels, on a barrier whose
+// phase completes only if `arrive` (one thread arrives) -- otherwise nothing
+// ever completes it and the wait must give up after limit_ns and report.
+__global__ void k_wait_probe(int arrive, uint64_t limit_ns, int* status)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (arrive && threadIdx.x == 0) mbar_arrive(&bar);
+    const bool ok = mbar_wait_bounded(&bar, 0, limit_ns);
+    if (threadIdx.x == 0) *status = ok ? R2P_OK : R2P_ETIMEOUT;
+}
+
+cudaError_t launch_wait_probe(int arrive, uint64_t limit_ns, int* d_status, cudaStream_t s)
+{
+    k_wait_probe<<<1, 32, 0, s>>>(arrive, limit_ns, d_status);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_bmp(DevImage* imgs, int n, uint32_t max_words, int nsm, cudaStream_t s)
 {
     const uint32_t want = (max_words + 255u) / 256u;

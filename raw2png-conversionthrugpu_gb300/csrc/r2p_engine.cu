@@ -1093,6 +1093,23 @@ static int deflate_bytes(r2p_engine* e, const void* d_in, size_t len, int level,
     return run(e, plans, cb, ST_DEFLATE, static_cast<cudaStream_t>(stream));
 }
 
+int r2p_selftest_bounded_wait(int device, int arrive, uint32_t limit_us, int* status)
+{
+    if (!status) return set_err(R2P_EINVAL, "NULL argument");
+    if (limit_us == 0 || limit_us > 1000000u) return set_err(R2P_EINVAL, "limit_us must be in [1, 1000000]");
+    R2P_CU(cudaSetDevice(device), "cudaSetDevice");
+    int* d = nullptr;
+    R2P_CU(cudaMalloc(&d, sizeof(int)), "cudaMalloc");
+    int h = -1;
+    cudaError_t ce = cudaMemset(d, 0xFF, sizeof(int));
+    if (ce == cudaSuccess) ce = launch_wait_probe(arrive ? 1 : 0, (uint64_t)limit_us * 1000ull, d, nullptr);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (ce != cudaSuccess) return cuda_err(ce, "bounded-wait probe");
+    *status = h;
+    return R2P_OK;
+}
+
 int r2p_adler32_device(r2p_engine* e, const void* d_data, size_t len, uint32_t* d_result, void* stream)
 {
     if (!e || (!d_data && len) || !d_result) return set_err(R2P_EINVAL, "NULL argument");

@@ -11,6 +11,9 @@ void note_launch();
 
 // k_filter.cu
 cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s);
+// The bounded barrier wait on a barrier nothing completes (arrive = 0) or
+// one arrival completes (arrive = 1); writes R2P_ETIMEOUT or R2P_OK.
+cudaError_t launch_wait_probe(int arrive, uint64_t limit_ns, int* d_status, cudaStream_t s);
 // BMP files of n images (max_words: 4-byte words of the largest file).
 cudaError_t launch_bmp(DevImage* imgs, int n, uint32_t max_words, int nsm, cudaStream_t s);
 cudaError_t launch_window_filter(DevImage* imgs, const BandItem* items, int nitems, int grid,
