@@ -139,7 +139,9 @@ void   r2p_batch_destroy(r2p_batch* b);
 
 /* Size-class tuning: per class of raw image bytes (sorted, the last class
  * takes everything larger), the DEFLATE block size used when an image's
- * block_size is 0, the filter's rows per work item (0 = from occupancy) and
+ * block_size is 0, the filter's rows per work item (0 = about 64 KB of
+ * filtered output per item; a work list with fewer items than resident CTA
+ * slots is split evenly over them instead) and
  * the LZ77 hash-table bits per image (9 or 10: 2^9 or 2^10 entries per
  * warp).  Set from the
  * autotuner's table; n = 0 restores the built-in one.  Replaces the fixed

@@ -91,12 +91,12 @@ struct ImgPlan {
     uint64_t png_bound = 0;
     int smem = 0;      // filter smem wanted
     int lreg = 0;      // worst-case LUT region
-    int band_rows = 0; // rows per filter work item (0 = from occupancy)
+    int band_rows = 0; // rows per filter work item (0 = about 64 KB of filtered output)
     int hash_bits = 10;
 };
 
-// Built-in size-class table (every class: 64 KiB blocks, bands from
-// occupancy, 2^11-entry LZ77 hash tables); engines may load an autotuned one.
+// Built-in size-class table (every class: 64 KiB blocks, bands of about 64 KB
+// of filtered output, 2^10-entry LZ77 hash tables); engines may load an autotuned one.
 static const std::vector<r2p_tuning> kDefaultTuning = {{~0ull, kBlock64, 0, 10}};
 
 static const r2p_tuning& tune_for(const std::vector<r2p_tuning>& t, uint64_t raw_bytes)
