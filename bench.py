@@ -209,7 +209,8 @@ def measure_c3(r2p, W, eng, stream, n=1000, reps=3):
     return res
 
 
-def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4, threads=4, slots=4):
+def measure_c4(r2p, W, n_pool=48, per_level=960, levels=(0.5, 0.8, 1.0), seed=4, threads=4, slots=8,
+               batch_cap=0, batch_bytes=0):
     """Served request stream: Poisson arrivals at fractions of the measured
     saturation rate; p50/p99 latency (submit -> PNG in host memory) and images/s,
     next to the plain per-image path (r2p_encode_png, one image at a time)."""
@@ -242,7 +243,8 @@ def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4,
         plain(img, pin)
     plain_ips = len(pool) / (time.perf_counter() - t0)
     eng.close()
-    sv = r2p.Server(0, hbm_budget=40 << 30, host_pool_bytes=8 << 30, max_inflight_batches=slots)
+    sv = r2p.Server(0, hbm_budget=40 << 30, host_pool_bytes=8 << 30, max_inflight_batches=slots,
+                    max_batch_images=batch_cap, max_batch_bytes=batch_bytes)
     try:
         with open(TUNING_JSON) as f:
             sv.set_tuning([tuple(c) for c in json.load(f)["classes"]])
@@ -264,22 +266,36 @@ def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4,
                 img, pin = pool[i % len(pool)]
                 tickets[i] = sv.submit(img, pin, borrow=True)
 
+        lat = [None] * n
+        failed = []
+
+        def waiter():
+            # a client that takes each result as it completes (wait + release
+            # in submission order), so finished PNGs do not pile up in the
+            # server's pinned pool while the burst is still arriving
+            for i in range(n):
+                while tickets[i] is None:
+                    time.sleep(0.0001)
+                st, png_len, l, q = sv.wait(tickets[i], timeout_ms=120000, fetch=False)
+                if st != r2p.OK or not png_len:
+                    failed.append((tickets[i], st))
+                lat[i] = l
+
         ths = [threading.Thread(target=submitter, args=(k,)) for k in range(threads)]
+        wt = threading.Thread(target=waiter)
         for t in ths:
             t.start()
+        wt.start()
         for t in ths:
             t.join()
-        lat = []
-        for t in tickets:
-            st, png_len, l, q = sv.wait(t, timeout_ms=120000, fetch=False)
-            if st != r2p.OK or not png_len:
-                raise RuntimeError(f"served request {t} ended with status {st}")
-            lat.append(l)
+        wt.join()
+        if failed:
+            raise RuntimeError(f"served requests failed: {failed[:4]}")
         wall = time.perf_counter() - start
         return lat, wall
 
     # saturation: everything arrives at once; median of three bursts of 2x the
-    # per-level count (one burst lasts only ~0.1 s)
+    # per-level count
     run([0.0] * 64)
     bursts = []
     for _ in range(3):
@@ -289,6 +305,7 @@ def measure_c4(r2p, W, n_pool=48, per_level=480, levels=(0.5, 0.8, 1.0), seed=4,
     sats = [b[0] for b in bursts]
     sat, st = sorted(bursts, key=lambda b: b[0])[1]
     out = {"requests_per_level": per_level, "pool_images": len(pool), "mean_raw_bytes": int(mean_raw), "slots": slots,
+           "max_batch_images": batch_cap or 512, "max_batch_bytes": batch_bytes or (96 << 20),
            "plain_images_per_s": round(plain_ips, 1), "saturation_images_per_s": round(sat, 1),
            "saturation_runs_images_per_s": [round(x, 1) for x in sats],
            "saturation_vs_plain": round(sat / plain_ips, 2), "mean_batch_images_at_saturation":

@@ -260,8 +260,12 @@ typedef struct r2p_server r2p_server;
 typedef struct r2p_server_config {
     size_t hbm_budget;            /* device bytes for requests + scratch (0 = 40 GiB) */
     size_t host_pool_bytes;       /* pinned host bytes for pixels + PNGs (0 = 4 GiB) */
-    int    max_inflight_batches;  /* concurrent batches / streams (0 = 3) */
+    int    max_inflight_batches;  /* concurrent batches / streams (0 = 8) */
     int    max_batch_images;      /* requests per batch at most (0 = 512) */
+    size_t max_batch_bytes;       /* raw pixel bytes per batch at most, a single larger
+                                     request excepted (0 = 96 MiB): small batches keep
+                                     the streams' uploads, kernels and downloads
+                                     overlapped */
 } r2p_server_config;
 typedef struct r2p_result {
     int            status;        /* R2P_OK, R2P_ECANCELED, or the failure */

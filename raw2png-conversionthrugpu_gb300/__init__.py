@@ -77,7 +77,8 @@ class Tuning(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget", ctypes.c_size_t), ("host_pool_bytes", ctypes.c_size_t),
-                ("max_inflight_batches", ctypes.c_int), ("max_batch_images", ctypes.c_int)]
+                ("max_inflight_batches", ctypes.c_int), ("max_batch_images", ctypes.c_int),
+                ("max_batch_bytes", ctypes.c_size_t)]
 
 
 class Result(ctypes.Structure):
@@ -593,8 +594,9 @@ class Batch:
 class Server:
     """Continuous-batching request server (r2p_server)."""
 
-    def __init__(self, device=0, hbm_budget=0, host_pool_bytes=0, max_inflight_batches=0, max_batch_images=0):
-        cfg = ServerConfig(hbm_budget, host_pool_bytes, max_inflight_batches, max_batch_images)
+    def __init__(self, device=0, hbm_budget=0, host_pool_bytes=0, max_inflight_batches=0, max_batch_images=0,
+                 max_batch_bytes=0):
+        cfg = ServerConfig(hbm_budget, host_pool_bytes, max_inflight_batches, max_batch_images, max_batch_bytes)
         p = _vp()
         check(lib().r2p_server_create(device, ctypes.byref(cfg), ctypes.byref(p)))
         self.h = p.value

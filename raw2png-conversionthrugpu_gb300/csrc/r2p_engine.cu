@@ -1640,9 +1640,10 @@ static bool launch_batch(r2p_server* sv, Slot& sl)
     CallBuffers cb;
     {
         std::lock_guard<std::mutex> lk(sv->mu);
-        size_t est = 0;
+        size_t est = 0, raw_total = 0;
         while (!sv->pending.empty() && (int)take.size() < sv->cfg.max_batch_images) {
             Request* r = sv->pending.front();
+            if (!take.empty() && raw_total + r->raw_bytes > sv->cfg.max_batch_bytes) break;
             // admission: its pixels + PNG now, and room for its scratch later
             if (!sv->dpool.alloc(r->d_bytes, r->d_off)) break;
             if (sv->dpool.cap() - sv->dpool.used() < est + r->est_scratch) {
@@ -1650,6 +1651,7 @@ static bool launch_batch(r2p_server* sv, Slot& sl)
                 break;
             }
             est += r->est_scratch;
+            raw_total += r->raw_bytes;
             sv->pending.pop_front();
             take.push_back(r);
         }
@@ -1788,8 +1790,9 @@ int r2p_server_create(int device, const r2p_server_config* cfg, r2p_server** out
     if (cfg) c = *cfg;
     if (c.hbm_budget == 0) c.hbm_budget = (size_t)40 << 30;
     if (c.host_pool_bytes == 0) c.host_pool_bytes = (size_t)4 << 30;
-    if (c.max_inflight_batches <= 0) c.max_inflight_batches = 3;
+    if (c.max_inflight_batches <= 0) c.max_inflight_batches = 8;
     if (c.max_batch_images <= 0) c.max_batch_images = 512;
+    if (c.max_batch_bytes == 0) c.max_batch_bytes = (size_t)96 << 20;
     r2p_engine* e = nullptr;
     int rc = r2p_engine_create(device, 0, &e);
     if (rc) return rc;

@@ -91,7 +91,7 @@ bool encode_folder(const char* input_dir, const char* output_dir, const Pipeline
     std::memset(&sc, 0, sizeof(sc));
     sc.hbm_budget = (size_t)8 << 30;
     sc.host_pool_bytes = (size_t)2 << 30;
-    sc.max_inflight_batches = 3;
+    sc.max_inflight_batches = 8;
     sc.max_batch_images = 256;
     r2p_server* srv = nullptr;
     if (!r2p_host::ok(r2p_server_create(cfg.device, &sc, &srv), "r2p_server_create")) return false;
