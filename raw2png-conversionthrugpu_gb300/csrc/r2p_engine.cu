@@ -602,13 +602,21 @@ static int bind(r2p_engine* e)
 
 }  // namespace r2p
 
-struct r2p_batch {
-    r2p_engine* eng = nullptr;
-    int n = 0;
+// One part of a batch: its own work list and memory, launched as its own
+// branch of the batch's graph.
+struct BatchPart {
     std::vector<ImgPlan> plans;
     CallBuffers cb;
     Prepared P;
-    uint8_t* mem = nullptr;           // descriptors + tables + scratch, owned
+    size_t off = 0;                   // of the part's descriptors + scratch in mem
+};
+
+struct r2p_batch {
+    r2p_engine* eng = nullptr;
+    int n = 0;
+    std::vector<BatchPart> parts;
+    uint8_t* mem = nullptr;           // descriptors + tables + scratch of every part, owned
+    size_t total = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -1206,6 +1214,13 @@ int r2p_engine_get_tuning(r2p_engine* e, int cap, r2p_tuning* out, int* n)
     return R2P_OK;
 }
 
+// Batches of at least this many images are split into kBatchParts parts
+// (size-balanced: images dealt out by decreasing size) whose stage kernels
+// run as parallel branches of one graph, so one part's stage tails overlap
+// another's work; each image's bytes do not depend on its part.
+constexpr int kBatchParts = 4;
+constexpr int kBatchSplitMin = 64;
+
 int r2p_batch_create(r2p_engine* e, int n, const r2p_image* imgs, const void* const* d_pixels, void* const* d_pngs,
                      const size_t* png_caps, uint64_t* d_png_lens, r2p_batch** out)
 {
@@ -1215,40 +1230,57 @@ int r2p_batch_create(r2p_engine* e, int n, const r2p_image* imgs, const void* co
     std::lock_guard<std::mutex> lk(e->mu);
     int rc = bind(e);
     if (rc) return rc;
+    std::vector<ImgPlan> all((size_t)n);
+    for (int i = 0; i < n; i++) {
+        rc = plan_image(imgs[i], 0, all[i], e->tuning);
+        if (!rc && png_caps[i] < all[i].png_bound) rc = set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
+        if (!rc && (!d_pixels[i] || !d_pngs[i])) rc = set_err(R2P_EINVAL, "NULL buffer");
+        if (rc) return rc;
+    }
+    const int K = n >= kBatchSplitMin ? kBatchParts : 1;
+    std::vector<int> order((size_t)n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return all[x].raw_bytes > all[y].raw_bytes; });
     r2p_batch* b = new r2p_batch();
     b->eng = e;
     b->n = n;
-    b->plans.resize((size_t)n);
-    for (int i = 0; i < n; i++) {
-        rc = plan_image(imgs[i], 0, b->plans[i], e->tuning);
-        if (!rc && png_caps[i] < b->plans[i].png_bound) rc = set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
-        if (!rc && (!d_pixels[i] || !d_pngs[i])) rc = set_err(R2P_EINVAL, "NULL buffer");
-        if (rc) { delete b; return rc; }
-        b->cb.raw.push_back(static_cast<const uint8_t*>(d_pixels[i]));
-        b->cb.filt.push_back(nullptr);
-        b->cb.prior.push_back(nullptr);
-        b->cb.out.push_back(static_cast<uint8_t*>(d_pngs[i]));
-        b->cb.out_cap.push_back(png_caps[i]);
-        b->cb.out_len.push_back(d_png_lens + i);
+    b->parts.resize((size_t)K);
+    for (int j = 0; j < n; j++) {
+        const int i = order[j];
+        BatchPart& pt = b->parts[(size_t)(j % K)];
+        pt.plans.push_back(all[i]);
+        pt.cb.raw.push_back(static_cast<const uint8_t*>(d_pixels[i]));
+        pt.cb.filt.push_back(nullptr);
+        pt.cb.prior.push_back(nullptr);
+        pt.cb.out.push_back(static_cast<uint8_t*>(d_pngs[i]));
+        pt.cb.out_cap.push_back(png_caps[i]);
+        pt.cb.out_len.push_back(d_png_lens + i);
     }
-    plan_work(e, b->plans, b->cb, 0, b->P);
-    if (e->budget && b->P.total > e->budget) {
+    for (BatchPart& pt : b->parts) {
+        plan_work(e, pt.plans, pt.cb, 0, pt.P);
+        pt.off = b->total;
+        b->total += align_up(pt.P.total, 256);
+    }
+    if (e->budget && b->total > e->budget) {
         delete b;
         return set_err(R2P_EBUDGET, "batch exceeds the engine's HBM budget");
     }
-    cudaError_t ce = cudaMalloc(&b->mem, b->P.total);
+    cudaError_t ce = cudaMalloc(&b->mem, b->total);
     if (ce != cudaSuccess) {
         delete b;
         return cuda_err(ce, "batch cudaMalloc");
     }
-    fill_pointers(b->plans, b->cb, b->P, b->mem);
-    std::vector<uint8_t> host(b->P.desc_bytes);
-    write_descriptors(host.data(), b->plans, b->P);
-    ce = cudaMemcpy(b->mem, host.data(), b->P.desc_bytes, cudaMemcpyHostToDevice);
-    if (ce != cudaSuccess) {
-        cudaFree(b->mem);
-        delete b;
-        return cuda_err(ce, "batch descriptor upload");
+    for (BatchPart& pt : b->parts) {
+        fill_pointers(pt.plans, pt.cb, pt.P, b->mem + pt.off);
+        std::vector<uint8_t> host(pt.P.desc_bytes);
+        write_descriptors(host.data(), pt.plans, pt.P);
+        ce = cudaMemcpy(b->mem + pt.off, host.data(), pt.P.desc_bytes, cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) {
+            cudaFree(b->mem);
+            delete b;
+            return cuda_err(ce, "batch descriptor upload");
+        }
     }
     *out = b;
     return R2P_OK;
@@ -1259,7 +1291,56 @@ int r2p_batch_launch(r2p_batch* b, void* stream)
     if (!b) return set_err(R2P_EINVAL, "NULL batch");
     int rc = bind(b->eng);
     if (rc) return rc;
-    return launch_stages(b->eng, b->n, b->P, b->mem, ST_ALL, static_cast<cudaStream_t>(stream), nullptr, nullptr);
+    for (BatchPart& pt : b->parts) {
+        rc = launch_stages(b->eng, (int)pt.plans.size(), pt.P, b->mem + pt.off, ST_ALL,
+                           static_cast<cudaStream_t>(stream), nullptr, nullptr);
+        if (rc) return rc;
+    }
+    return R2P_OK;
+}
+
+// Capture every part's stage kernels into one graph: part 0 on the capture
+// stream, the others on forked streams joined back before the capture ends.
+static int capture_batch(r2p_batch* b, cudaStream_t cs)
+{
+    const int K = (int)b->parts.size();
+    std::vector<cudaStream_t> fs((size_t)K, nullptr);
+    std::vector<cudaEvent_t> ev((size_t)K, nullptr);
+    int rc = R2P_OK;
+    cudaError_t ce = cudaSuccess;
+    for (int k = 0; k < K && ce == cudaSuccess; k++) {
+        ce = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+        if (ce == cudaSuccess && k > 0) ce = cudaStreamCreateWithFlags(&fs[k], cudaStreamNonBlocking);
+    }
+    if (ce == cudaSuccess) ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+        fs[0] = cs;
+        if (K > 1) ce = cudaEventRecord(ev[0], cs);
+        for (int k = 1; k < K && ce == cudaSuccess; k++) ce = cudaStreamWaitEvent(fs[k], ev[0], 0);
+        for (int k = 0; k < K && ce == cudaSuccess && !rc; k++)
+            rc = launch_stages(b->eng, (int)b->parts[k].plans.size(), b->parts[k].P, b->mem + b->parts[k].off,
+                               ST_ALL, fs[k], nullptr, nullptr);
+        for (int k = 1; k < K && ce == cudaSuccess && !rc; k++) {
+            ce = cudaEventRecord(ev[k], fs[k]);
+            if (ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, ev[k], 0);
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce2 = cudaStreamEndCapture(cs, &g);
+        if (ce == cudaSuccess) ce = ce2;
+        if (!rc && ce == cudaSuccess) {
+            b->graph = g;
+            ce = cudaGraphInstantiate(&b->exec, g, 0);
+        } else if (g) {
+            cudaGraphDestroy(g);
+        }
+    }
+    for (int k = 1; k < K; k++)
+        if (fs[k]) cudaStreamDestroy(fs[k]);
+    for (auto x : ev)
+        if (x) cudaEventDestroy(x);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_err(ce, "graph capture");
+    return R2P_OK;
 }
 
 int r2p_batch_launch_graph(r2p_batch* b, void* stream)
@@ -1272,28 +1353,16 @@ int r2p_batch_launch_graph(r2p_batch* b, void* stream)
         // capture on a private stream so the caller's stream state is untouched
         cudaStream_t cs;
         R2P_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
-        cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (ce == cudaSuccess) {
-            rc = launch_stages(b->eng, b->n, b->P, b->mem, ST_ALL, cs, nullptr, nullptr);
-            cudaGraph_t g = nullptr;
-            ce = cudaStreamEndCapture(cs, &g);
-            if (!rc && ce == cudaSuccess) {
-                b->graph = g;
-                ce = cudaGraphInstantiate(&b->exec, g, 0);
-            } else if (g) {
-                cudaGraphDestroy(g);
-            }
-        }
+        rc = capture_batch(b, cs);
         cudaStreamDestroy(cs);
         if (rc) return rc;
-        if (ce != cudaSuccess) return cuda_err(ce, "graph capture");
     }
     R2P_CU(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
-    note_launch_graph(b->P.any_stored, b->P.any_lz, b->P.any_dyn);
+    for (const BatchPart& pt : b->parts) note_launch_graph(pt.P.any_stored, pt.P.any_lz, pt.P.any_dyn);
     return R2P_OK;
 }
 
-size_t r2p_batch_device_bytes(const r2p_batch* b) { return b ? b->P.total : 0; }
+size_t r2p_batch_device_bytes(const r2p_batch* b) { return b ? b->total : 0; }
 
 void r2p_batch_destroy(r2p_batch* b)
 {

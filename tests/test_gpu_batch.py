@@ -100,3 +100,28 @@ def test_dynamic_level_batch_equals_alone(engine, O, r2p, W):
     for i in range(len(imgs)):
         decode_and_check(O, r2p, imgs[i], raws[i], batched[i])
         assert engine.encode_png(imgs[i], raws[i]) == batched[i], specs[i]
+
+
+def test_split_batch_graph_equals_alone(engine, O, r2p, W):
+    # 80 images: the batch runs as four size-balanced parts, parallel branches
+    # of one graph; every file must equal the image encoded alone
+    rng = np.random.default_rng(5)
+    specs = [(int(rng.integers(16, 400)), int(rng.integers(4, 300)), float(rng.uniform(-300, 300)),
+              float(rng.uniform(80, 1500))) for _ in range(80)]
+    imgs, raws, bufs, outs, caps, lens = make_batch_inputs(r2p, W, specs, level=1)
+    for i in range(0, len(imgs), 3):
+        imgs[i].level = 6 if i % 2 else 0
+        caps[i] = r2p.png_bound(imgs[i])
+        outs[i] = r2p.DeviceBuffer(caps[i])
+    b = engine.batch(imgs, [x.ptr for x in bufs], [o.ptr for o in outs], caps, lens.ptr)
+    b.launch_graph()
+    graphed = read_all(outs, lens, len(imgs))
+    for o in outs:
+        o.memset(0)
+    b.launch()
+    assert read_all(outs, lens, len(imgs)) == graphed
+    b.close()
+    for i in range(len(imgs)):
+        assert engine.encode_png(imgs[i], raws[i]) == graphed[i], specs[i]
+        if i % 10 == 0:
+            decode_and_check(O, r2p, imgs[i], raws[i], graphed[i])
