@@ -45,11 +45,12 @@ def test_inflate_exact(engine, name, data, level):
         assert len(z) <= data.size + 5 * (data.size // 65520 + 1) + 6     # stored blocks
 
 
+@pytest.mark.parametrize("level", [1, 6])
 @pytest.mark.parametrize("bs", [1024, 4096, 32752, 65520])
-def test_block_sizes(engine, bs):
+def test_block_sizes(engine, bs, level):
     rng = np.random.default_rng(bs)
     data = np.repeat(rng.integers(0, 16, size=30000, dtype=np.uint8), 7)
-    z = engine.zlib_compress(data, 1, block_size=bs)
+    z = engine.zlib_compress(data, level, block_size=bs)
     assert zlib.decompress(z) == data.tobytes()
 
 
