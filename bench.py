@@ -132,6 +132,18 @@ def ncu_traffic(kernel, workload):
     return int(m.group(1)) if m else None
 
 
+def ncu_issue(kernel, workload):
+    """Issue-active fraction of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"issue_active_per_launch:\s*%s\s+%s\s*=\s*([0-9.]+)" % (re.escape(kernel), re.escape(workload)),
+                  text)
+    return float(m.group(1)) if m else None
+
+
 TUNING_JSON = os.path.join(ROOT, "raw2png-conversionthrugpu_gb300", "tuning_gb300.json")
 
 
@@ -655,6 +667,12 @@ def run_ours(args):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    issue = ncu_issue(kname, args.workload)
+    if issue is not None:
+        line["roofline"]["issue_active"] = issue
+        line["roofline"]["issue_note"] = ("fraction of cycles the kernel's schedulers issued an instruction "
+                                          "(ncu, profiles/ncu_traffic.md): the kernel is bound by instruction "
+                                          "issue, with DRAM traffic equal to its input once")
     line["config"]["tuning"] = tuning
     if args.workload in ("c1", "c2"):
         line["dynamic_huffman"] = measure_dynamic(r2p, img, engines, streams, d_raw, nvar, min(args.steps, 300))
