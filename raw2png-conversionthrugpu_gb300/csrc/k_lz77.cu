@@ -13,15 +13,21 @@
 // shared memory).  Every one of the CTA's 1024 threads parses its own
 // 68-byte sub-range of the block sequentially (32 warps per SM: the parse is
 // latency-bound, so the warps hide each other's dependency chains) -- a
-// greedy LZ77 with three candidates per position: distance 1 (a run), the
-// same column one scanline up, and the head of a 4-byte hash table shared by
-// the 32 lanes of a warp (seeded from the ~2 KB before the warp's range).
-// Matches may reach any earlier byte of the block within 32 KB but end inside
-// the thread's sub-range, and are extended by word compares.  Each thread
-// packs its fixed-Huffman codes LSB-first into a 64-bit register (codes from
-// per-CTA tables) and spills whole words to a private shared-memory buffer
-// (an odd word stride keeps the 32 lanes on distinct banks), so no atomics
-// are needed while parsing.  A CTA-wide scan of the per-thread bit counts
+// greedy LZ77 with two candidates per position: distance 1 (a run) and the
+// head of a 4-byte hash table shared by the 32 lanes of a warp (seeded from
+// the ~2 KB before the warp's range).  The PNG filter has already taken the
+// scanline above out of the bytes, so a third candidate one scanline up found
+// almost nothing the hash did not (990 of 12.55 M bytes on a 3072x3072 16-bit
+// image) and cost a tenth of the launch; it is not searched.
+// Matches reach back into the warp's range and the history hashed before it
+// but end inside the thread's sub-range; runs are extended by aligned word
+// compares against the repeated byte, other matches by unaligned word
+// compares.  Each thread packs its fixed-Huffman codes LSB-first into a 64-bit
+// register (codes from per-CTA tables) and spills whole words to a private
+// shared-memory buffer (an odd word stride keeps the 32 lanes on distinct
+// banks), so no atomics are needed while parsing; each thread then adds up
+// the Adler-32 sums of its sub-range, so warps that finish early do that work.
+// A CTA-wide scan of the per-thread bit counts
 // places the bitstreams behind the 3-bit block header; an end-of-block code
 // and an empty stored block byte-align the output, so blocks are independent
 // and join by plain concatenation.  A block whose Huffman form would not be
@@ -45,12 +51,15 @@ constexpr uint32_t FULL = 0xFFFFFFFFu;
 // Bytes each thread parses: a multiple of 4 whose word count is odd, so the 32
 // lanes of a warp, reading at the same offset of their sub-ranges, hit 32
 // distinct shared-memory banks.  Output words per thread use an odd stride too.
-__host__ __device__ inline int lz_sub_bytes(int block_size)
+__host__ __device__ constexpr int lz_sub_bytes(int block_size)
 {
     const int w = ((block_size + kLzThreads - 1) / kLzThreads + 3) >> 2;
     return 4 * (w | 1);
 }
 __host__ __device__ inline int lz_lane_words(int block_size) { return ((lz_sub_bytes(block_size) * 9 + 31) / 32) | 1; }
+// A warp's hash table holds positions of its own range and of the history
+// hashed before it, so every candidate lies within the 32 KB window.
+static_assert(32 * lz_sub_bytes(kBlock64) + kPrefill <= kMaxDist, "hash candidates stay within the window");
 __host__ __device__ inline int lz_in_bytes(int block_size) { return ((block_size + 15) & ~15) + 64; }
 
 static int lz_smem_bytes(int block_size, int hash_bits)
@@ -140,60 +149,58 @@ __device__ __forceinline__ void match_code(int len, int dist, const uint32_t* lt
     n = (int)(cl + lne + 5 + dne);
 }
 
-// 4 bytes at i >= -3 with bytes at negative indices read as zero.
-__device__ __forceinline__ uint32_t ld32z(const uint8_t* base, int i)
-{
-    if (i >= 0) return ld32u(base, i);
-    return i > -4 ? ld32u(base, 0) << (8 * -i) : 0u;
-}
-
 // Greedy parse of in[s, e) by one thread into the word buffer `ob`.
 // `tab` is the warp's shared hash table (latest position + 1 per hash).
 // Returns the number of bits written; the last partial word is stored too.
 //
-// The thread keeps three sliding registers -- w (bytes p..p+3), the byte
-// before p, and wv (bytes p-rb1..p-rb1+3, the scanline above) -- so a literal
-// step reads one new byte per stream instead of two words per candidate.
-__device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb, uint16_t* tab, uint32_t* ob,
+// The thread keeps two sliding registers -- w (bytes p..p+3) and the byte
+// before p -- so a literal step reads one new byte.
+__device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t* tab, uint32_t* ob,
                                const uint32_t* lt, const uint32_t* dt)
 {
-    const bool vert = rb1 > 1 && rb1 <= kMaxDist;
     uint64_t acc = 0;
     int nacc = 0, nw = 0;
-    uint32_t bits = 0;
     int p = s;
     // sliding state for position p (bytes past the block end read the zero padding)
     uint32_t w = ld32u(in, p);
     // at the block start no run can match: a "previous byte" unequal to w's first byte
     uint32_t prev = p > 0 ? (uint32_t)in[p - 1] : ((w & 0xFFu) ^ 1u);
-    // exact once p >= rb1 (the only positions it is compared at)
-    uint32_t wv = vert ? ld32z(in, max(p - rb1, -4)) : 0u;
-    while (p < e) {
+    while (p + 4 <= e) {
         int L = 0, D = 0;
-        if (p + 4 <= e) {
+        {
             const uint32_t h = hash4(w, hb);
             const int t = tab[h];
             tab[h] = (uint16_t)(p + 1);
             if (w == prev * 0x01010101u) {
                 D = 1;
-            } else if (vert && p >= rb1 && wv == w) {
-                D = rb1;
             } else if (t) {
-                const int dist = p - (t - 1);
-                if (dist > 0 && dist <= kMaxDist && ld32u(in, t - 1) == w) D = dist;
+                const int dist = p - (t - 1);       // <= 0: a later position of another lane
+                if (dist > 0 && ld32u(in, t - 1) == w) D = dist;
             }
             if (D) {
                 // extend by words, then bytes, up to the sub-range end
                 const int maxl = min(kMaxMatch, e - p);
-                const int c = p - D;
-                L = 4;
-                bool more = true;
-                while (more && L + 4 <= maxl) {
-                    const uint32_t x = ld32u(in, c + L) ^ ld32u(in, p + L);
-                    if (x) { L += (__ffs(x) - 1) >> 3; more = false; }
-                    else L += 4;
+                if (D == 1) {
+                    // a run: aligned words against the byte replicated
+                    const uint32_t rep = prev * 0x01010101u;
+                    const uint32_t* in32 = reinterpret_cast<const uint32_t*>(in);
+                    const int i = p + 4, lim = p + maxl;
+                    int q = i >> 2;
+                    uint32_t x = (in32[q] ^ rep) & (0xFFFFFFFFu << (8 * (i & 3)));
+                    while (!x && 4 * q + 4 < lim) x = in32[++q] ^ rep;
+                    const int end = x ? 4 * q + ((__ffs(x) - 1) >> 3) : 4 * q + 4;
+                    L = min(end, lim) - p;
+                } else {
+                    const int c = p - D;
+                    L = 4;
+                    bool more = true;
+                    while (more && L + 4 <= maxl) {
+                        const uint32_t x = ld32u(in, c + L) ^ ld32u(in, p + L);
+                        if (x) { L += (__ffs(x) - 1) >> 3; more = false; }
+                        else L += 4;
+                    }
+                    while (more && L < maxl && in[c + L] == in[p + L]) L++;
                 }
-                while (more && L < maxl && in[c + L] == in[p + L]) L++;
             }
         }
         uint32_t v;
@@ -203,20 +210,26 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb,
             p += L;
             w = ld32u(in, p);
             prev = in[p - 1];
-            wv = vert ? ld32z(in, max(p - rb1, -4)) : 0u;
         } else {
             lit_code(w & 0xFFu, v, nb);
             prev = w & 0xFFu;
             w = (w >> 8) | ((uint32_t)in[p + 4] << 24);
-            if (vert) {
-                const int q = p + 4 - rb1;
-                wv = (wv >> 8) | ((uint32_t)(q >= 0 ? in[q] : 0) << 24);
-            }
             p += 1;
         }
         acc |= (uint64_t)v << nacc;
         nacc += nb;
-        bits += (uint32_t)nb;
+        if (nacc >= 32) {
+            ob[nw++] = (uint32_t)acc;
+            acc >>= 32;
+            nacc -= 32;
+        }
+    }
+    for (; p < e; p++) {                        // the last bytes: literals
+        uint32_t v;
+        int nb;
+        lit_code(in[p], v, nb);
+        acc |= (uint64_t)v << nacc;
+        nacc += nb;
         if (nacc >= 32) {
             ob[nw++] = (uint32_t)acc;
             acc >>= 32;
@@ -224,7 +237,7 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int rb1, int hb,
         }
     }
     if (nacc > 0) ob[nw] = (uint32_t)acc;
-    return bits;
+    return (uint32_t)(nw * 32 + nacc);
 }
 
 // Adler sums of n bytes in shared memory (whole CTA).
@@ -262,7 +275,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     uint16_t* tabs = reinterpret_cast<uint16_t*>(outs + kLzThreads * lw);
     __shared__ uint64_t red64[kLzWarps];
     __shared__ uint32_t red32[kLzWarps];
-    __shared__ uint32_t wsum[kLzWarps];
+    __shared__ uint32_t wsum[kLzWarps], wa1[kLzWarps], wa2[kLzWarps];
     __shared__ uint32_t s_info[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __shared__ uint32_t s_len[kLenTab], s_dist[kDistTab];
@@ -292,9 +305,6 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         for (int i = n + tid; i < in_bytes; i += kLzThreads) in[i] = 0;
         for (int i = tid; i < (kLzWarps << hb) / 2; i += kLzThreads) reinterpret_cast<uint32_t*>(tabs)[i] = 0u;
         __syncthreads();
-        uint32_t s1;
-        uint64_t s2;
-        cta_adler_sums<kLzThreads>(in, n, s1, s2, red64);
         // seed the warp's table from the bytes before its range, oldest first
         const int sub = lz_sub_bytes(n);
         const int ws0 = min(n, warp * 32 * sub);
@@ -306,7 +316,27 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         }
         // parse this thread's sub-range
         const int s = min(n, tid * sub), e = min(n, s + sub);
-        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, d.rb + 1, hb, mytab, myout, s_len, s_dist) : 0u;
+        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, hb, mytab, myout, s_len, s_dist) : 0u;
+        // Adler sums of the sub-range, taken while slower warps still parse:
+        // S1 = sum d_i, S2 = sum (n - i) d_i mod 65521 (< 2^31 before the
+        // reduction: at most 17 words of weight <= 65520)
+        uint32_t a1 = 0, a2 = 0;
+        {
+            const int e4 = s + ((e - s) & ~3);
+            for (int i = s; i < e4; i += 4) {
+                const uint32_t v = reinterpret_cast<const uint32_t*>(in)[i >> 2];
+                const uint32_t bs = bytesum4(v);
+                a1 += bs;
+                a2 += (uint32_t)(n - i) * bs - bytewsum4(v);
+            }
+            for (int i = e4; i < e; i++) {
+                a1 += in[i];
+                a2 += (uint32_t)(n - i) * in[i];
+            }
+            a2 %= kAdlerMod;
+        }
+        a1 = __reduce_add_sync(FULL, a1);
+        a2 = __reduce_add_sync(FULL, a2);
         // CTA-wide exclusive scan of the bit counts
         uint32_t incl = nbits;
 #pragma unroll
@@ -314,7 +344,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             const uint32_t y = __shfl_up_sync(FULL, incl, o);
             if (lane >= o) incl += y;
         }
-        if (lane == 31) wsum[warp] = incl;
+        if (lane == 31) { wsum[warp] = incl; wa1[warp] = a1; wa2[warp] = a2; }
         __syncthreads();
         uint32_t wbase = 0, tot = 3;
         for (int k = 0; k < kLzWarps; k++) {
@@ -372,6 +402,8 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             crc = gf2_mulmod(crc_small(hdr, kStoredHdr, ctab), xpow8n((uint64_t)n, xpow)) ^ cd;
         }
         if (tid == 0) {
+            uint32_t s1 = 0, s2 = 0;
+            for (int k = 0; k < kLzWarps; k++) { s1 += wa1[k]; s2 += wa2[k]; }
             bo.out_len = huff ? huff : (uint32_t)(n + kStoredHdr);
             bo.crc = crc;
             bo.s1 = s1;
