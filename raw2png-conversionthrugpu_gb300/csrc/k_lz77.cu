@@ -309,9 +309,16 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         const int sub = lz_sub_bytes(n);
         const int ws0 = min(n, warp * 32 * sub);
         const int prefill = min(kPrefill, d.block_size / kLzWarps);    // ~one warp range of history
-        for (int q0 = max(0, ws0 - prefill); q0 < ws0; q0 += 32) {
-            const int q = q0 + lane;
-            if (q < ws0 && q + 4 <= n) mytab[hash4(ld32u(in, q), hb)] = (uint16_t)(q + 1);
+        // four positions per lane per step, from two aligned words
+        for (int q0 = max(0, ws0 - prefill) & ~3; q0 < ws0; q0 += 128) {
+            const int q = q0 + 4 * lane;
+            if (q < ws0) {
+                const uint32_t* w32 = reinterpret_cast<const uint32_t*>(in);
+                const uint32_t lo = w32[q >> 2], hi = w32[(q >> 2) + 1];
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (q + j + 4 <= n) mytab[hash4(fshr(lo, hi, 8u * j), hb)] = (uint16_t)(q + j + 1);
+            }
             __syncwarp();
         }
         // parse this thread's sub-range
@@ -370,12 +377,20 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             __syncthreads();
             const int nw = (int)((nbits + 31) / 32);
             const uint32_t sh = off & 31, q0 = off >> 5;
-            for (int j = 0; j < nw; j++) {
-                const uint32_t v = myout[j];
-                if (!v) continue;
-                // first and last words are shared with the neighbouring streams
-                atomicOr(&region[q0 + j], v << sh);
-                if (sh) atomicOr(&region[q0 + j + 1], v >> (32 - sh));
+            if (nw > 0) {
+                // the first and last words are shared with the neighbouring
+                // streams; the words between hold this stream's bits alone
+                uint32_t v = myout[0];
+                atomicOr(&region[q0], v << sh);
+                uint32_t carry = sh ? v >> (32 - sh) : 0u;
+                for (int j = 1; j < nw; j++) {
+                    v = myout[j];
+                    const uint32_t u = (v << sh) | carry;
+                    carry = sh ? v >> (32 - sh) : 0u;
+                    if (32u * (j + 1) <= sh + nbits) region[q0 + j] = u;     // whole word of this stream
+                    else atomicOr(&region[q0 + j], u);
+                }
+                if (sh) atomicOr(&region[q0 + nw], carry);
             }
             if (tid == 0) atomicOr(&region[0], last ? 3u : 2u);     // BFINAL, BTYPE = 01
             __syncthreads();
