@@ -173,8 +173,8 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t
             tab[h] = (uint16_t)(p + 1);
             if (w == prev * 0x01010101u) {
                 D = 1;
-            } else if (t) {
-                const int dist = p - (t - 1);       // <= 0: a later position of another lane
+            } else {
+                const int dist = p - (t - 1);       // <= 0: a later position of another lane, or empty
                 if (dist > 0 && ld32u(in, t - 1) == w) D = dist;
             }
             if (D) {
@@ -303,7 +303,8 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             for (int i = tid; i < n; i += kLzThreads) in[i] = src[i];
         }
         for (int i = n + tid; i < in_bytes; i += kLzThreads) in[i] = 0;
-        for (int i = tid; i < (kLzWarps << hb) / 2; i += kLzThreads) reinterpret_cast<uint32_t*>(tabs)[i] = 0u;
+        // empty entries hold 0xFFFF: position 65534, never before p (p < 65520)
+        for (int i = tid; i < (kLzWarps << hb) / 2; i += kLzThreads) reinterpret_cast<uint32_t*>(tabs)[i] = 0xFFFFFFFFu;
         __syncthreads();
         // seed the warp's table from the bytes before its range, oldest first
         const int sub = lz_sub_bytes(n);
