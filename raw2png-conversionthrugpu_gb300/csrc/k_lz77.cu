@@ -150,7 +150,8 @@ __device__ __forceinline__ void match_code(int len, int dist, const uint32_t* lt
 }
 
 // Greedy parse of in[s, e) by one thread into the word buffer `ob`.
-// `tab` is the warp's shared hash table (latest position + 1 per hash).
+// `tab` is the warp's shared hash table (latest position + 1 per hash;
+// 0xFFFF when empty, a position no candidate can precede).
 // Returns the number of bits written; the last partial word is stored too.
 //
 // The thread keeps two sliding registers -- w (bytes p..p+3) and the byte
@@ -371,7 +372,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         uint8_t* slot = scratch + (size_t)b * slot_bytes;
         uint32_t crc;
         if (huff) {
-            // place the 512 bitstreams behind the 3-bit header, into `in`
+            // place the 1024 bitstreams behind the 3-bit header, into `in`
             uint32_t* region = reinterpret_cast<uint32_t*>(in);
             const int rwords = (int)((huff + 3) / 4) + 2;
             for (int i = tid; i < rwords; i += kLzThreads) region[i] = 0;
