@@ -10,9 +10,11 @@
 // Only inflate-equality is required of the compressed bytes.
 //
 // Design.  One CTA per DEFLATE block (<= 65520 filtered bytes, staged in
-// shared memory).  Every one of the CTA's 1024 threads parses its own
-// 68-byte sub-range of the block sequentially (32 warps per SM: the parse is
-// latency-bound, so the warps hide each other's dependency chains) -- a
+// shared memory): 1024 threads for blocks above 32 KB (one CTA per SM), 512
+// for blocks up to 32 KB (two CTAs per SM, so one CTA's barrier phases run
+// beside the other's parse).  Every thread parses its own 68-byte sub-range
+// of the block sequentially (32 warps per SM: the parse is latency-bound, so
+// the warps hide each other's dependency chains) -- a
 // greedy LZ77 with two candidates per position: distance 1 (a run) and the
 // head of a 4-byte hash table shared by the 32 lanes of a warp (seeded from
 // the ~2 KB before the warp's range).  The PNG filter has already taken the
@@ -48,24 +50,34 @@ constexpr int kMaxDist = 32768;
 constexpr int kMaxMatch = 258;
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 
-// Bytes each thread parses: a multiple of 4 whose word count is odd, so the 32
-// lanes of a warp, reading at the same offset of their sub-ranges, hit 32
-// distinct shared-memory banks.  Output words per thread use an odd stride too.
-__host__ __device__ constexpr int lz_sub_bytes(int block_size)
+// Bytes each thread parses in a block of n bytes: a multiple of 4 whose word
+// count is odd, so the 32 lanes of a warp, reading at the same offset of their
+// sub-ranges, hit 32 distinct shared-memory banks; 68 for blocks above 32 KB
+// (at most 964 threads busy), n / 512 rounded up that way below.  It depends
+// on the block alone, not on the CTA size a launch picks, so a block encodes
+// to the same bytes in any batch.
+__host__ __device__ constexpr int lz_sub_bytes(int n)
 {
-    const int w = ((block_size + kLzThreads - 1) / kLzThreads + 3) >> 2;
+    const int m = n < 32768 ? n : 32768;
+    const int w = ((m + 511) / 512 + 3) >> 2;
     return 4 * (w | 1);
 }
-__host__ __device__ inline int lz_lane_words(int block_size) { return ((lz_sub_bytes(block_size) * 9 + 31) / 32) | 1; }
+// Output words per thread: an odd stride (distinct banks for the 32 lanes)
+// for the 1024-thread CTA; the 512-thread CTA drops that word so that two
+// CTAs fit one SM's shared memory (its lanes' spills meet in pairs).
+__host__ __device__ inline int lz_lane_words(int block_size, int nt = kLzThreads)
+{
+    return ((lz_sub_bytes(block_size) * 9 + 31) / 32) | (nt == kLzThreads ? 1 : 0);
+}
 // A warp's hash table holds positions of its own range and of the history
 // hashed before it, so every candidate lies within the 32 KB window.
 static_assert(32 * lz_sub_bytes(kBlock64) + kPrefill <= kMaxDist, "hash candidates stay within the window");
 __host__ __device__ inline int lz_in_bytes(int block_size) { return ((block_size + 15) & ~15) + 64; }
 
-static int lz_smem_bytes(int block_size, int hash_bits)
+static int lz_smem_bytes(int block_size, int hash_bits, int nt = kLzThreads)
 {
-    return 4096 + lz_in_bytes(block_size) + kLzThreads * lz_lane_words(block_size) * 4 +
-           kLzWarps * (1 << hash_bits) * 2 + 256;
+    return 4096 + lz_in_bytes(block_size) + nt * lz_lane_words(block_size, nt) * 4 +
+           (nt / 32) * (1 << hash_bits) * 2 + 256;
 }
 
 uint64_t lz77_slot_bytes(int block_size) { return (uint64_t)((block_size + kStoredHdr + 64 + 255) & ~255); }
@@ -263,7 +275,8 @@ __device__ void cta_adler_sums(const uint8_t* buf, int n, uint32_t& s1_out, uint
     s2_out = cta_sum64<NT>(s2, red64);
 }
 
-__global__ void __launch_bounds__(kLzThreads, 1)
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT)
 k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int max_block,
               uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
 {
@@ -271,18 +284,18 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     uint32_t (*ctab)[256] = reinterpret_cast<uint32_t (*)[256]>(sm);
     uint8_t* in = sm + 4096;
     const int in_bytes = lz_in_bytes(max_block);
-    const int lw = lz_lane_words(max_block);
+    const int lw = lz_lane_words(max_block, NT);
     uint32_t* outs = reinterpret_cast<uint32_t*>(in + in_bytes);
-    uint16_t* tabs = reinterpret_cast<uint16_t*>(outs + kLzThreads * lw);
-    __shared__ uint64_t red64[kLzWarps];
-    __shared__ uint32_t red32[kLzWarps];
-    __shared__ uint32_t wsum[kLzWarps], wa1[kLzWarps], wa2[kLzWarps];
+    uint16_t* tabs = reinterpret_cast<uint16_t*>(outs + NT * lw);
+    __shared__ uint64_t red64[(NT / 32)];
+    __shared__ uint32_t red32[(NT / 32)];
+    __shared__ uint32_t wsum[(NT / 32)], wa1[(NT / 32)], wa2[(NT / 32)];
     __shared__ uint32_t s_info[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __shared__ uint32_t s_len[kLenTab], s_dist[kDistTab];
     build_crc_tables(ctab);
-    for (int i = threadIdx.x; i < kLenTab; i += kLzThreads) s_len[i] = len_entry(i + 3);
-    for (int i = threadIdx.x; i < kDistTab; i += kLzThreads) s_dist[i] = dist_entry(i);
+    for (int i = threadIdx.x; i < kLenTab; i += NT) s_len[i] = len_entry(i + 3);
+    for (int i = threadIdx.x; i < kDistTab; i += NT) s_dist[i] = dist_entry(i);
     uint32_t* myout = outs + tid * lw;
 
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
@@ -297,20 +310,20 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         __syncthreads();
         // stage the block (+ zero padding), clear the hash tables
         if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-            for (int i = tid; i < (n >> 4); i += kLzThreads)
+            for (int i = tid; i < (n >> 4); i += NT)
                 reinterpret_cast<uint4*>(in)[i] = __ldg(reinterpret_cast<const uint4*>(src) + i);
-            for (int i = (n & ~15) + tid; i < n; i += kLzThreads) in[i] = src[i];
+            for (int i = (n & ~15) + tid; i < n; i += NT) in[i] = src[i];
         } else {
-            for (int i = tid; i < n; i += kLzThreads) in[i] = src[i];
+            for (int i = tid; i < n; i += NT) in[i] = src[i];
         }
-        for (int i = n + tid; i < in_bytes; i += kLzThreads) in[i] = 0;
+        for (int i = n + tid; i < in_bytes; i += NT) in[i] = 0;
         // empty entries hold 0xFFFF: position 65534, never before p (p < 65520)
-        for (int i = tid; i < (kLzWarps << hb) / 2; i += kLzThreads) reinterpret_cast<uint32_t*>(tabs)[i] = 0xFFFFFFFFu;
+        for (int i = tid; i < ((NT / 32) << hb) / 2; i += NT) reinterpret_cast<uint32_t*>(tabs)[i] = 0xFFFFFFFFu;
         __syncthreads();
         // seed the warp's table from the bytes before its range, oldest first
         const int sub = lz_sub_bytes(n);
         const int ws0 = min(n, warp * 32 * sub);
-        const int prefill = min(kPrefill, d.block_size / kLzWarps);    // ~one warp range of history
+        const int prefill = min(kPrefill, 32 * sub);          // one warp range of history
         // four positions per lane per step, from two aligned words
         for (int q0 = max(0, ws0 - prefill) & ~3; q0 < ws0; q0 += 128) {
             const int q = q0 + 4 * lane;
@@ -356,7 +369,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         if (lane == 31) { wsum[warp] = incl; wa1[warp] = a1; wa2[warp] = a2; }
         __syncthreads();
         uint32_t wbase = 0, tot = 3;
-        for (int k = 0; k < kLzWarps; k++) {
+        for (int k = 0; k < (NT / 32); k++) {
             if (k < warp) wbase += wsum[k];
             tot += wsum[k];
         }
@@ -375,7 +388,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             // place the 1024 bitstreams behind the 3-bit header, into `in`
             uint32_t* region = reinterpret_cast<uint32_t*>(in);
             const int rwords = (int)((huff + 3) / 4) + 2;
-            for (int i = tid; i < rwords; i += kLzThreads) region[i] = 0;
+            for (int i = tid; i < rwords; i += NT) region[i] = 0;
             __syncthreads();
             const int nw = (int)((nbits + 31) / 32);
             const uint32_t sh = off & 31, q0 = off >> 5;
@@ -405,22 +418,22 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             __syncthreads();
             uint32_t s1d;
             uint64_t s2d;
-            cta_crc_adler<kLzThreads>(in, (int)huff, false, ctab, xpow, crc, s1d, s2d, red64, red32);
+            cta_crc_adler<NT>(in, (int)huff, false, ctab, xpow, crc, s1d, s2d, red64, red32);
             const uint4* s4 = reinterpret_cast<const uint4*>(in);
-            for (int i = tid; i < (int)((huff + 15) / 16); i += kLzThreads) reinterpret_cast<uint4*>(slot)[i] = s4[i];
+            for (int i = tid; i < (int)((huff + 15) / 16); i += NT) reinterpret_cast<uint4*>(slot)[i] = s4[i];
         } else {
             uint8_t hdr[kStoredHdr] = {(uint8_t)(last ? 1 : 0), (uint8_t)(n & 0xFF), (uint8_t)(n >> 8),
                                        (uint8_t)(~n & 0xFF), (uint8_t)((~n >> 8) & 0xFF)};
             if (tid < kStoredHdr) slot[tid] = hdr[tid];
-            cta_copy_to_global<kLzThreads>(slot + kStoredHdr, in, n);
+            cta_copy_to_global<NT>(slot + kStoredHdr, in, n);
             uint32_t cd, s1d;
             uint64_t s2d;
-            cta_crc_adler<kLzThreads>(in, n, false, ctab, xpow, cd, s1d, s2d, red64, red32);
+            cta_crc_adler<NT>(in, n, false, ctab, xpow, cd, s1d, s2d, red64, red32);
             crc = gf2_mulmod(crc_small(hdr, kStoredHdr, ctab), xpow8n((uint64_t)n, xpow)) ^ cd;
         }
         if (tid == 0) {
             uint32_t s1 = 0, s2 = 0;
-            for (int k = 0; k < kLzWarps; k++) { s1 += wa1[k]; s2 += wa2[k]; }
+            for (int k = 0; k < (NT / 32); k++) { s1 += wa1[k]; s2 += wa2[k]; }
             bo.out_len = huff ? huff : (uint32_t)(n + kStoredHdr);
             bo.crc = crc;
             bo.s1 = s1;
@@ -1009,10 +1022,19 @@ cudaError_t launch_dyn(const DevImage* imgs, BlockOut* blocks, int nblocks, int 
 cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block, uint8_t* scratch,
                         uint64_t slot_bytes, const uint32_t* xpow, int grid, int hash_bits, cudaStream_t s)
 {
-    const int smem = lz_smem_bytes(max_block, hash_bits == 9 ? 9 : 10);
-    cudaError_t e = cudaFuncSetAttribute(k_lz77_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    k_lz77_blocks<<<grid, kLzThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    const int hb = hash_bits == 9 ? 9 : 10;
+    cudaError_t e;
+    if (max_block <= 32768) {           // two 512-thread CTAs per SM
+        const int smem = lz_smem_bytes(max_block, hb, 512);
+        e = cudaFuncSetAttribute(k_lz77_blocks<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_lz77_blocks<512><<<grid, 512, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    } else {
+        const int smem = lz_smem_bytes(max_block, hb);
+        e = cudaFuncSetAttribute(k_lz77_blocks<kLzThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_lz77_blocks<kLzThreads><<<grid, kLzThreads, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    }
     note_launch();
     return cudaGetLastError();
 }
