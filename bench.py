@@ -3,7 +3,8 @@
 A step is one pass of the encode path over one image of the workload.  The
 default workload is a single 3072x3072 uint16 image (12 bits stored, DICOM
 PS3.3 window WC 2048 / WW 4096 to 16-bit output, adaptive filter, LZ77 +
-fixed Huffman at level 1 in 65520-byte blocks).  Eight distinct inputs are
+fixed Huffman at level 1 in independent blocks, of the size the autotuned
+size-class table gives: config.block_size).  Eight distinct inputs are
 rotated so the working set (151 MB of raw pixels) exceeds the 129 MB L2.
 
   value     device-resident throughput: pixels and PNG in HBM, timed with CUDA
@@ -40,7 +41,7 @@ UNIT = "MB/s"
 def workload_desc(name):
     return {
         "c1": "single 3072x3072 uint16 image (12 bits stored), DICOM window WC 2048/WW 4096 to 16-bit, "
-              "adaptive filter, LZ77 + fixed Huffman level 1, 65520-byte independent blocks",
+              "adaptive filter, LZ77 + fixed Huffman level 1 in independent blocks (config.block_size)",
         "c0": "single 512x512 uint16 CT phantom (12 bits stored), slope 1 / intercept -1024, WC 40/WW 400 to "
               "8-bit (Q15 path), adaptive filter, stored DEFLATE (level 0)",
         "c2": "single 6000x4000 RGB uint16 image, no window, adaptive filter, LZ77 + fixed Huffman level 1",
@@ -156,6 +157,20 @@ def load_tuning(eng):
         return "autotuned (%s)" % os.path.basename(TUNING_JSON)
     except (OSError, KeyError, ValueError):
         return "built-in"
+
+
+def block_size_used(eng, img):
+    """DEFLATE block size the engine's table gives this image: the class's
+    size at level 1, 65520 at other levels, unless the image sets its own."""
+    if img.block_size:
+        return img.block_size
+    if img.level != 1:
+        return 65520
+    classes = eng.get_tuning()
+    for (max_raw, bs, _, _) in classes:
+        if img.raw_bytes <= max_raw:
+            return bs
+    return classes[-1][1]
 
 
 def measure_c3(r2p, W, eng, stream, n=1000, reps=3):
@@ -674,6 +689,7 @@ def run_ours(args):
                                           "(ncu, profiles/ncu_traffic.md): the kernel is bound by instruction "
                                           "issue, with DRAM traffic equal to its input once")
     line["config"]["tuning"] = tuning
+    line["config"]["block_size"] = block_size_used(engines[0], img)
     if args.workload in ("c1", "c2"):
         line["dynamic_huffman"] = measure_dynamic(r2p, img, engines, streams, d_raw, nvar, min(args.steps, 300))
     if not args.no_batched:

@@ -138,8 +138,10 @@ size_t r2p_batch_device_bytes(const r2p_batch* b);
 void   r2p_batch_destroy(r2p_batch* b);
 
 /* Size-class tuning: per class of raw image bytes (sorted, the last class
- * takes everything larger), the DEFLATE block size used when an image's
- * block_size is 0, the filter's rows per work item (0 = about 64 KB of
+ * takes everything larger), the DEFLATE block size used for a level-1 image
+ * whose block_size is 0 (levels 0 and 2-9 keep 65520-byte blocks: fewer
+ * stored headers, and per-block Huffman codes that pay for their header),
+ * the filter's rows per work item (0 = about 64 KB of
  * filtered output per item; a work list with fewer items than resident CTA
  * slots is split evenly over them instead) and
  * the LZ77 hash-table bits per image (9 or 10: 2^9 or 2^10 entries per

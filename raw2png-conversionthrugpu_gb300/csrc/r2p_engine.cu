@@ -160,7 +160,9 @@ static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip,
     d.level = im.level;
     const uint64_t raw_total = pitch * im.height;
     const r2p_tuning& tc = tune_for(tune, raw_total);
-    int bs = im.block_size ? im.block_size : tc.block_size;
+    // the tuned block size is the LZ77 kernel's; stored and dynamic-Huffman
+    // blocks stay as large as DEFLATE allows unless the image says otherwise
+    int bs = im.block_size ? im.block_size : im.level == 1 ? tc.block_size : kBlock64;
     ip.band_rows = tc.band_rows;
     ip.hash_bits = tc.hash_bits;
     if (bs < 1024 || bs > kBlock64 || (bs & 15)) return set_err(R2P_EINVAL, "block_size must be a multiple of 16 in [1024, 65520]");

@@ -73,6 +73,20 @@ def test_tuning_table_changes_blocks_not_pixels(O, r2p, W):
     eng.close()
 
 
+def test_tuned_block_size_applies_to_level_1_only(engine, r2p, W):
+    """The table's block size is the LZ77 kernel's: a level-1 image follows it,
+    stored (level 0) and dynamic-Huffman (level 6) images keep 65520-byte
+    blocks, so their bytes match an engine with the built-in table."""
+    eng = r2p.Engine(0)
+    eng.set_tuning([(2 ** 62, 4096, 0, 10)])
+    raw = W.ct_phantom(77, 640, 480)
+    for level in (0, 1, 6):
+        img = W.image_ct8(640, 480, 40.0, 400.0, level=level)
+        same = eng.encode_png(img, raw) == engine.encode_png(img, raw)
+        assert same == (level != 1), level
+    eng.close()
+
+
 def test_mixed_tuning_classes_same_as_alone(O, r2p, W):
     """Images of different size classes (different block sizes and LZ77 table
     sizes) in one batch give the same bytes as each image encoded alone."""
