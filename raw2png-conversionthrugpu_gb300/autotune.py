@@ -17,7 +17,7 @@ import sys
 import numpy as np
 
 CLASSES = [(256, 256), (512, 512), (1024, 1024), (2048, 2500), (3072, 3072)]
-CANDIDATES = [(bs, br, hb) for bs in (65520, 32752) for hb in (10, 9) for br in (0, 16, 32, 64, 128)]
+CANDIDATES = [(bs, br, hb) for bs in (65520, 32752, 21760) for hb in (10, 9) for br in (0, 16, 32, 64, 128)]
 DEFAULT_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_gb300.json")
 
 
@@ -125,7 +125,7 @@ def pick_table(r2p, W, per_class, log=print):
     eng = r2p.Engine(0)
     stream = r2p.Stream()
     tables = {"per-class": per_class}
-    for bs in (65520, 32752):
+    for bs in (65520, 32752, 21760):
         tables["all %d" % bs] = [(c[0], bs, c[2], c[3]) for c in per_class]
     best = None
     for name, t in tables.items():

@@ -11,8 +11,9 @@
 //
 // Design.  One CTA per DEFLATE block (<= 65520 filtered bytes, staged in
 // shared memory): 1024 threads for blocks above 32 KB (one CTA per SM), 512
-// for blocks up to 32 KB (two CTAs per SM, so one CTA's barrier phases run
-// beside the other's parse).  Every thread parses its own 68-byte sub-range
+// for blocks up to 32 KB (two CTAs per SM) and 320 for blocks up to 21760
+// bytes (three CTAs per SM), so that one CTA's barrier phases run beside the
+// others' parses.  Every thread parses its own 68-byte sub-range
 // of the block sequentially (32 warps per SM: the parse is latency-bound, so
 // the warps hide each other's dependency chains) -- a
 // greedy LZ77 with two candidates per position: distance 1 (a run) and the
@@ -52,19 +53,19 @@ constexpr uint32_t FULL = 0xFFFFFFFFu;
 
 // Bytes each thread parses in a block of n bytes: a multiple of 4 whose word
 // count is odd, so the 32 lanes of a warp, reading at the same offset of their
-// sub-ranges, hit 32 distinct shared-memory banks; 68 for blocks above 32 KB
-// (at most 964 threads busy), n / 512 rounded up that way below.  It depends
-// on the block alone, not on the CTA size a launch picks, so a block encodes
-// to the same bytes in any batch.
+// sub-ranges, hit 32 distinct shared-memory banks; 68 for blocks above 21760
+// bytes (at most 320, 482 or 964 threads busy in the three CTA sizes), n / 320
+// rounded up that way below.  It depends on the block alone, not on the CTA
+// size a launch picks, so a block encodes to the same bytes in any batch.
 __host__ __device__ constexpr int lz_sub_bytes(int n)
 {
-    const int m = n < 32768 ? n : 32768;
-    const int w = ((m + 511) / 512 + 3) >> 2;
+    const int m = n < 21760 ? n : 21760;
+    const int w = ((m + 319) / 320 + 3) >> 2;
     return 4 * (w | 1);
 }
 // Output words per thread: an odd stride (distinct banks for the 32 lanes)
-// for the 1024-thread CTA; the 512-thread CTA drops that word so that two
-// CTAs fit one SM's shared memory (its lanes' spills meet in pairs).
+// for the 1024-thread CTA; the smaller CTAs drop that word so that two or
+// three CTAs fit one SM's shared memory (their lanes' spills meet in pairs).
 __host__ __device__ inline int lz_lane_words(int block_size, int nt = kLzThreads)
 {
     return ((lz_sub_bytes(block_size) * 9 + 31) / 32) | (nt == kLzThreads ? 1 : 0);
@@ -1024,7 +1025,12 @@ cudaError_t launch_lz77(const DevImage* imgs, BlockOut* blocks, int nblocks, int
 {
     const int hb = hash_bits == 9 ? 9 : 10;
     cudaError_t e;
-    if (max_block <= 32768) {           // two 512-thread CTAs per SM
+    if (max_block <= 21760) {           // three 320-thread CTAs per SM
+        const int smem = lz_smem_bytes(max_block, hb, 320);
+        e = cudaFuncSetAttribute(k_lz77_blocks<320>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_lz77_blocks<320><<<grid, 320, smem, s>>>(imgs, blocks, nblocks, max_block, scratch, slot_bytes, xpow);
+    } else if (max_block <= 32768) {           // two 512-thread CTAs per SM
         const int smem = lz_smem_bytes(max_block, hb, 512);
         e = cudaFuncSetAttribute(k_lz77_blocks<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
