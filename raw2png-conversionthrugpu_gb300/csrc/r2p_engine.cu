@@ -301,6 +301,10 @@ struct r2p_engine {
     std::vector<r2p_engine*> helpers;
     uint64_t* many_lens = nullptr;
     cudaEvent_t many_ev[R2P_MANY_SLOTS] = {};
+    // per slot: the PNG download runs on its own stream, so the next image's
+    // upload overlaps it; the next image's kernels wait for its event
+    cudaStream_t many_dl[R2P_MANY_SLOTS] = {};
+    cudaEvent_t many_dl_ev[R2P_MANY_SLOTS] = {};
     std::mutex mu;
     // stage timing (events between stage launches on the call's stream)
     bool timing = false;
@@ -698,6 +702,13 @@ void r2p_engine_destroy(r2p_engine* e)
         cudaStreamDestroy(e->hstream);
     }
     for (r2p_engine* h : e->helpers) r2p_engine_destroy(h);
+    for (int k = 0; k < R2P_MANY_SLOTS; k++) {
+        if (e->many_dl[k]) {
+            cudaStreamSynchronize(e->many_dl[k]);
+            cudaStreamDestroy(e->many_dl[k]);
+        }
+        if (e->many_dl_ev[k]) cudaEventDestroy(e->many_dl_ev[k]);
+    }
     for (auto ev : e->many_ev)
         if (ev) cudaEventDestroy(ev);
     if (e->many_lens) cudaFreeHost(e->many_lens);
@@ -845,8 +856,11 @@ int r2p_encode_png_many(r2p_engine* e, int n, const r2p_image* imgs, const void*
         e->helpers.push_back(h);
     }
     if (!e->many_lens) R2P_CU(cudaMallocHost(&e->many_lens, sizeof(uint64_t) * K), "cudaMallocHost");
-    for (int k = 0; k < K; k++)
+    for (int k = 0; k < K; k++) {
         if (!e->many_ev[k]) R2P_CU(cudaEventCreateWithFlags(&e->many_ev[k], cudaEventDisableTiming), "event");
+        if (!e->many_dl[k]) R2P_CU(cudaStreamCreateWithFlags(&e->many_dl[k], cudaStreamNonBlocking), "stream");
+        if (!e->many_dl_ev[k]) R2P_CU(cudaEventCreateWithFlags(&e->many_dl_ev[k], cudaEventDisableTiming), "event");
+    }
     // plan every image first and size the helpers' arenas once: an arena must
     // not move while an earlier image's PNG download from it is queued
     std::vector<ImgPlan> plans(n);
@@ -877,6 +891,8 @@ int r2p_encode_png_many(r2p_engine* e, int n, const r2p_image* imgs, const void*
     struct Inflight {
         int img = -1;
         uint8_t* d_png = nullptr;
+        bool dl = false;                  // a download from this slot's PNG region is queued
+        size_t dl_len = 0;
     };
     std::vector<Inflight> fl(K);
     // the PNG of slot k's image: its length is on the host once the event fired
@@ -899,8 +915,12 @@ int r2p_encode_png_many(r2p_engine* e, int n, const r2p_image* imgs, const void*
             st[j] = set_err(R2P_ENOSPC, "png_cap too small for the encoded PNG");
             return;
         }
-        const cudaError_t c2 = cudaMemcpyAsync(h_pngs[j], fl[k].d_png, (size_t)len, cudaMemcpyDeviceToHost, h->hstream);
+        // the length event fired, so the kernels that wrote the PNG are done
+        cudaError_t c2 = cudaMemcpyAsync(h_pngs[j], fl[k].d_png, (size_t)len, cudaMemcpyDeviceToHost, e->many_dl[k]);
+        if (c2 == cudaSuccess) c2 = cudaEventRecord(e->many_dl_ev[k], e->many_dl[k]);
         if (c2 != cudaSuccess) st[j] = cuda_err(c2, "png download");
+        fl[k].dl = true;
+        fl[k].dl_len = (size_t)len;
     };
     auto enqueue = [&](int k, int i) -> int {
         r2p_engine* h = e->helpers[k];
@@ -920,7 +940,13 @@ int r2p_encode_png_many(r2p_engine* e, int n, const r2p_image* imgs, const void*
         uint8_t* d_png = ext + raw_region;
         uint64_t* d_len = reinterpret_cast<uint64_t*>(d_png + png_region);
         cb.raw = {d_raw}; cb.out = {d_png}; cb.out_len = {d_len};
+        // the slot's previous PNG may still be downloading: the upload may run
+        // beside it when it lands elsewhere in the arena (images of one size
+        // share a layout), the kernels only after it
+        const bool clash = fl[k].dl && d_raw < fl[k].d_png + fl[k].dl_len && fl[k].d_png < d_raw + raw_bytes;
+        if (clash) R2P_CU(cudaStreamWaitEvent(s, e->many_dl_ev[k], 0), "order download");
         R2P_CU(cudaMemcpyAsync(d_raw, h_pixels[i], raw_bytes, cudaMemcpyHostToDevice, s), "pixel upload");
+        if (fl[k].dl && !clash) R2P_CU(cudaStreamWaitEvent(s, e->many_dl_ev[k], 0), "order download");
         r = launch(h, one, cb, P, ST_ALL, s);
         if (r) return r;
         R2P_CU(cudaMemcpyAsync(e->many_lens + k, d_len, sizeof(uint64_t), cudaMemcpyDeviceToHost, s), "length");
@@ -940,8 +966,10 @@ int r2p_encode_png_many(r2p_engine* e, int n, const r2p_image* imgs, const void*
     }
     for (int k = 0; k < K; k++)
         if (fl[k].img >= 0) finish(k);
-    for (r2p_engine* h : e->helpers) {
-        const cudaError_t ce = cudaStreamSynchronize(h->hstream);
+    for (int k = 0; k < K; k++) {
+        r2p_engine* h = e->helpers[k];
+        cudaError_t ce = cudaStreamSynchronize(h->hstream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->many_dl[k]);
         if (ce != cudaSuccess && !first_err) first_err = cuda_err(ce, "sync");
     }
     for (int i = 0; i < n; i++) {

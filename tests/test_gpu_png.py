@@ -146,3 +146,25 @@ def test_encode_png_many_matches_single_calls(engine, O, r2p, W):
     for i in range(n - len(ring), n):                            # the last image written to each buffer
         got = bytes(ring[i % len(ring)].array[:lens[i]])
         assert got == engine.encode_png(imgs[i % 4], raws[i % 4])
+
+
+def test_encode_png_many_overlapping_downloads(engine, r2p, W):
+    """A slot's next upload may run beside its previous PNG download when the
+    two regions of the arena do not meet; sizes that change from image to
+    image move the regions, and every result must still equal its single
+    call (each image has its own pinned output buffer)."""
+    sizes = [(1500, 1200), (64, 48), (900, 1700), (1500, 1200), (300, 260), (2048, 700)]
+    imgs, raws = [], []
+    for i, (w, h) in enumerate(sizes):
+        imgs.append(W.image_ct16(w, h, 40.0, 400.0, level=1))
+        raws.append(W.ct_phantom(900 + i, w, h))
+    order = [(3 * i) % len(sizes) for i in range(4 * len(sizes))] + [0] * 8
+    pins = [r2p.PinnedBuffer(raws[j].nbytes) for j in range(len(sizes))]
+    for j, p in enumerate(pins):
+        p.array[:] = raws[j].view(np.uint8).reshape(-1)
+    outs = [r2p.PinnedBuffer(r2p.png_bound(imgs[j])) for j in order]
+    sts, lens = engine.encode_png_many([imgs[j] for j in order], [pins[j] for j in order], outs)
+    assert all(st == r2p.OK for st in sts)
+    single = [engine.encode_png(imgs[j], raws[j]) for j in range(len(sizes))]
+    for i, j in enumerate(order):
+        assert bytes(outs[i].array[:lens[i]]) == single[j], "image %d (size %s)" % (i, sizes[j])
