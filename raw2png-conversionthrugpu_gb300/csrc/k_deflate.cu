@@ -84,7 +84,7 @@ __device__ __forceinline__ void put_be32(uint8_t* p, uint32_t v)
     p[0] = (uint8_t)(v >> 24); p[1] = (uint8_t)(v >> 16); p[2] = (uint8_t)(v >> 8); p[3] = (uint8_t)v;
 }
 
-constexpr int kFinThreads = 256;
+constexpr int kFinThreads = 1024;   // one block per thread up to 1024 blocks: the GF(2) shifts run side by side
 
 // Exclusive scan of a per-thread u64 value across the CTA; returns the
 // exclusive prefix and writes the CTA total to *total.

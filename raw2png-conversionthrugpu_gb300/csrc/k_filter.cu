@@ -982,7 +982,7 @@ int filter_ctas_per_sm(int smem)
 
 cudaError_t launch_prepare_window(DevImage* imgs, int n, cudaStream_t s)
 {
-    k_prepare_window<<<n, 256, 0, s>>>(imgs, n);
+    k_prepare_window<<<n, 1024, 0, s>>>(imgs, n);      // 4096-entry tables: four entries per thread
     note_launch();
     return cudaGetLastError();
 }
