@@ -26,23 +26,47 @@ constexpr int kHdrWords = 144;
 // .. n-2, created in order of non-decreasing weight) keeps its weight in A[k]
 // until it is paired, then the index of its parent; the root n-2 keeps the
 // total weight.
+//
+// The two queue heads and the items behind them are kept in registers (wr,
+// wr1 for the internal nodes root, root + 1; wl, wl1 for the leaves leaf,
+// leaf + 1), so each comparison waits on no memory load: the GPU runs this
+// loop on one thread, where a load per comparison was the whole cost.  Node
+// root + 1 exists once root + 1 < next; the node made in this step becomes a
+// cached head when the queue in front of it is that short.  The leaves
+// ahead are never overwritten before they are taken (leaf >= next + 2).
 R2P_HD void mk_phase1(uint32_t* A, int n)
 {
     A[0] += A[1];
     int root = 0, leaf = 2;
+    uint32_t wr = A[0], wr1 = 0;
+    uint32_t wl = leaf < n ? A[leaf] : 0u, wl1 = leaf + 1 < n ? A[leaf + 1] : 0u;
     for (int next = 1; next < n - 1; next++) {
-        if (leaf >= n || A[root] < A[leaf]) {
-            A[next] = A[root];
+        uint32_t w;
+        if (leaf >= n || wr < wl) {                 // the queue is never empty here
+            w = wr;
             A[root++] = (uint32_t)next;
+            wr = wr1;
+            wr1 = root + 1 < next ? A[root + 1] : 0u;
         } else {
-            A[next] = A[leaf++];
+            w = wl;
+            leaf++;
+            wl = wl1;
+            wl1 = leaf + 1 < n ? A[leaf + 1] : 0u;
         }
-        if (leaf >= n || (root < next && A[root] < A[leaf])) {
-            A[next] += A[root];
+        if (leaf >= n || (root < next && wr < wl)) {
+            w += wr;
             A[root++] = (uint32_t)next;
+            wr = wr1;
+            wr1 = root + 1 < next ? A[root + 1] : 0u;
         } else {
-            A[next] += A[leaf++];
+            w += wl;
+            leaf++;
+            wl = wl1;
+            wl1 = leaf + 1 < n ? A[leaf + 1] : 0u;
         }
+        A[next] = w;
+        if (root == next) wr = w;
+        else if (root + 1 == next) wr1 = w;
     }
 }
 
