@@ -146,7 +146,10 @@ void   r2p_batch_destroy(r2p_batch* b);
  * slots is split evenly over them instead) and
  * the LZ77 hash-table bits per image (9 or 10: 2^9 or 2^10 entries per
  * warp).  Set from the
- * autotuner's table; n = 0 restores the built-in one.  Replaces the fixed
+ * autotuner's table; n = 0 restores the built-in one (the autotuner's GB300
+ * result: 21760-byte level-1 blocks in every class, band rows 16 / auto / 32
+ * / 32 / auto for classes up to 327680 / 1310720 / 6168576 / 14557184 raw
+ * bytes / larger, 10 hash bits).  Replaces the fixed
  * strip-height/pool-size defaults (src/main.cpp:165-170, src/pipeline.cpp:1587). */
 typedef struct r2p_tuning {
     uint64_t max_raw_bytes;

@@ -95,9 +95,15 @@ struct ImgPlan {
     int hash_bits = 10;
 };
 
-// Built-in size-class table (every class: 64 KiB blocks, bands of about 64 KB
-// of filtered output, 2^10-entry LZ77 hash tables); engines may load an autotuned one.
-static const std::vector<r2p_tuning> kDefaultTuning = {{~0ull, kBlock64, 0, 10}};
+// Built-in size-class table: the autotuner's result on GB300 (tuning_gb300.json,
+// written by autotune.py): 21760-byte level-1 blocks in every class (three LZ77
+// CTAs per SM), filter rows per work item by class, 2^10-entry hash tables.
+// Engines may load another table.
+static const std::vector<r2p_tuning> kDefaultTuning = {{327680, 21760, 16, 10},
+                                                       {1310720, 21760, 0, 10},
+                                                       {6168576, 21760, 32, 10},
+                                                       {14557184, 21760, 32, 10},
+                                                       {~0ull, 21760, 0, 10}};
 
 static const r2p_tuning& tune_for(const std::vector<r2p_tuning>& t, uint64_t raw_bytes)
 {
