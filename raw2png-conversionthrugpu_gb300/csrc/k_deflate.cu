@@ -62,7 +62,7 @@ k_stored_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks
         cta_crc_adler<kStoredThreads>(buf, n, true, tab, xpow, crc, s1, s2, red64, red32);
         if (tid == 0) {
             const uint32_t ch = crc_small(hdr, kStoredHdr, tab);
-            bo.crc = gf2_mulmod(ch, xpow8n((uint64_t)n, xpow)) ^ crc;
+            bo.crc = gf2_mulmod_t(ch, xpow8n_t((uint64_t)n, xpow, tab), tab) ^ crc;
             bo.out_len = (uint32_t)(n + kStoredHdr);
             bo.s1 = s1;
             bo.s2 = s2;
@@ -121,12 +121,8 @@ k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uin
     __shared__ uint64_t sw[kFinThreads / 32];
     __shared__ uint64_t red64[kFinThreads / 32];
     __shared__ uint32_t red32[kFinThreads / 32];
-    __shared__ uint32_t t0[256];
-    for (int n = threadIdx.x; n < 256; n += kFinThreads) {
-        uint32_t c = (uint32_t)n;
-        for (int k = 0; k < 8; k++) c = (c & 1u) ? kCrcPoly ^ (c >> 1) : c >> 1;
-        t0[n] = c;
-    }
+    __shared__ uint32_t tab[4][256];
+    build_crc_tables(tab);
     // 1. stream offsets
     uint64_t carry = 0;
     for (int base = 0; base < nb; base += kFinThreads) {
@@ -149,7 +145,7 @@ k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uin
         s1 += bo.s1;
         s2 = (s2 + bo.s2 % kAdlerMod + (after_in % kAdlerMod) * (bo.s1 % kAdlerMod)) % kAdlerMod;
         const uint64_t after_out = Ls - bo.out_off - bo.out_len + 4;   // + Adler trailer
-        cx ^= gf2_mulmod(bo.crc, xpow8n(after_out, xpow));
+        cx ^= gf2_mulmod_t(bo.crc, xpow8n_t(after_out, xpow, tab), tab);
     }
     s1 = cta_sum64<kFinThreads>(s1, red64);
     s2 = cta_sum64<kFinThreads>(s2, red64);
@@ -164,7 +160,7 @@ k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uin
             return;
         }
         const uint32_t adler = adler_from_sums(s1, s2 % kAdlerMod, F);
-        const uint32_t (*tab0)[256] = reinterpret_cast<const uint32_t (*)[256]>(t0);
+        const uint32_t (*tab0)[256] = tab;
         uint8_t* p = d.png;
         uint8_t head[6] = {'I', 'D', 'A', 'T', 0x78, zlib_flg(d.level)};
         uint8_t trl[4];
@@ -196,7 +192,7 @@ k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uin
         for (int i = 0; i < 6; i++) p[37 + i] = head[i];
         const uint32_t ch = crc_small(head, 6, tab0);
         const uint32_t ct = crc_small(trl, 4, tab0);
-        const uint32_t crc = gf2_mulmod(ch, xpow8n(Ls + 4, xpow)) ^ cx ^ ct;
+        const uint32_t crc = gf2_mulmod_t(ch, xpow8n_t(Ls + 4, xpow, tab), tab) ^ cx ^ ct;
         put_be32(q + 4, crc);
         const uint8_t iend[12] = {0, 0, 0, 0, 'I', 'E', 'N', 'D', 0xAE, 0x42, 0x60, 0x82};
         for (int i = 0; i < 12; i++) q[8 + i] = iend[i];

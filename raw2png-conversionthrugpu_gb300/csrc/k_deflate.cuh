@@ -55,6 +55,29 @@ __device__ __forceinline__ uint32_t crc_byte(uint32_t crc, uint32_t b, const uin
     return t[0][(crc ^ b) & 0xFF] ^ (crc >> 8);
 }
 
+// a * b mod P with the slicing tables at hand: the 63-bit carry-less
+// product (clmul32), moved up one bit, holds x^0..x^31 in its high word and
+// x^32..x^63 in its low word; the low word times x^32 is four zero bytes
+// through the CRC register (one crc_word step).  About 50 independent
+// instructions and four table reads, where gf2_mulmod is 32 dependent steps.
+__device__ __forceinline__ uint32_t gf2_mulmod_t(uint32_t a, uint32_t b, const uint32_t (*t)[256])
+{
+    const uint64_t r = clmul32(a, b) << 1;
+    return (uint32_t)(r >> 32) ^ crc_word((uint32_t)r, 0u, t);
+}
+
+// xpow8n with the table-assisted product.
+__device__ __forceinline__ uint32_t xpow8n_t(uint64_t n, const uint32_t* __restrict__ tab, const uint32_t (*t)[256])
+{
+    uint32_t r = __ldg(tab + (n & 1023));
+#pragma unroll
+    for (int l = 1; l < kXpowLevels; l++) {
+        const uint32_t j = (uint32_t)(n >> (10 * l)) & 1023u;
+        if (j) r = gf2_mulmod_t(r, __ldg(tab + l * 1024 + j), t);
+    }
+    return r;
+}
+
 // finalised crc32 of a few bytes (thread-local)
 __device__ __forceinline__ uint32_t crc_small(const uint8_t* p, int n, const uint32_t (*t)[256])
 {
@@ -91,22 +114,22 @@ __device__ __forceinline__ uint64_t cta_sum64(uint64_t v, uint64_t* red)
 
 // CRC-32 (finalised) of n bytes in shared memory `buf` (4-byte aligned), and
 // optionally the Adler sums S1 = sum d_i and S2 = sum (n - i) d_i.  Whole CTA.
-// Each thread takes contiguous kCrcChunk-byte chunks; chunk CRCs are shifted
-// to their place with a table lookup and at most four GF(2) products and
-// XOR-reduced.
-template <int NT>
+// Each thread takes contiguous CH-byte chunks (CH / 4 odd, so the lanes read
+// distinct banks); chunk CRCs are shifted to their place with a table lookup
+// and at most three table-assisted GF(2) products and XOR-reduced.
+template <int NT, int CH = kCrcChunk>
 __device__ void cta_crc_adler(const uint8_t* buf, int n, bool want_adler, const uint32_t (*t)[256],
                               const uint32_t* __restrict__ xpow, uint32_t& crc_out, uint32_t& s1_out,
                               uint64_t& s2_out, uint64_t* red64, uint32_t* red32)
 {
-    const int nch = (n + kCrcChunk - 1) / kCrcChunk;
+    const int nch = (n + CH - 1) / CH;
     const int last = nch - 1;
-    const int len_last = n - last * kCrcChunk;
+    const int len_last = n - last * CH;
     uint32_t crc_acc = 0;
     uint64_t s1 = 0, s2 = 0;
     for (int ch = threadIdx.x; ch < nch; ch += NT) {
-        const int o = ch * kCrcChunk;
-        const int L = (ch == last) ? len_last : kCrcChunk;
+        const int o = ch * CH;
+        const int L = (ch == last) ? len_last : CH;
         const uint32_t* w = reinterpret_cast<const uint32_t*>(buf + o);
         uint32_t c = 0xFFFFFFFFu;
         uint32_t cs1 = 0;
@@ -128,7 +151,7 @@ __device__ void cta_crc_adler(const uint8_t* buf, int n, bool want_adler, const 
         }
         c ^= 0xFFFFFFFFu;
         // shift past the bytes that follow this chunk
-        if (ch != last) c = gf2_mulmod(c, xpow8n((uint64_t)(n - o - L), xpow));
+        if (ch != last) c = gf2_mulmod_t(c, xpow8n_t((uint64_t)(n - o - L), xpow, t), t);
         crc_acc ^= c;
         if (want_adler) {
             const uint64_t after = (uint64_t)(n - o - L);

@@ -419,7 +419,8 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             __syncthreads();
             uint32_t s1d;
             uint64_t s2d;
-            cta_crc_adler<NT>(in, (int)huff, false, ctab, xpow, crc, s1d, s2d, red64, red32);
+            // 124-byte chunks: ~120 chains of 31 words for a 21760-byte block
+            cta_crc_adler<NT, 124>(in, (int)huff, false, ctab, xpow, crc, s1d, s2d, red64, red32);
             const uint4* s4 = reinterpret_cast<const uint4*>(in);
             for (int i = tid; i < (int)((huff + 15) / 16); i += NT) reinterpret_cast<uint4*>(slot)[i] = s4[i];
         } else {
@@ -430,7 +431,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
             uint32_t cd, s1d;
             uint64_t s2d;
             cta_crc_adler<NT>(in, n, false, ctab, xpow, cd, s1d, s2d, red64, red32);
-            crc = gf2_mulmod(crc_small(hdr, kStoredHdr, ctab), xpow8n((uint64_t)n, xpow)) ^ cd;
+            crc = gf2_mulmod_t(crc_small(hdr, kStoredHdr, ctab), xpow8n_t((uint64_t)n, xpow, ctab), ctab) ^ cd;
         }
         if (tid == 0) {
             uint32_t s1 = 0, s2 = 0;
@@ -979,7 +980,7 @@ k_rle_dyn_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ block
             uint32_t cd, s1d;
             uint64_t s2d;
             cta_crc_adler<kDynThreads>(in, n, false, ctab, xpow, cd, s1d, s2d, red64, red32);
-            crc = gf2_mulmod(crc_small(hdr, kStoredHdr, ctab), xpow8n((uint64_t)n, xpow)) ^ cd;
+            crc = gf2_mulmod_t(crc_small(hdr, kStoredHdr, ctab), xpow8n_t((uint64_t)n, xpow, ctab), ctab) ^ cd;
         }
         if (tid == 0) {
             bo.out_len = dyn ? dyn : (uint32_t)(n + kStoredHdr);

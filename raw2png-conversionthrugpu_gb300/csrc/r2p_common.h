@@ -207,7 +207,25 @@ R2P_HD int best_filter(const Score5& s)
 // ---------------------------------------------------------------------------
 constexpr uint32_t kCrcPoly = 0xEDB88320u;
 
-// a * b mod P (reflected representation).
+// Carry-less product of two 32-bit words (63 bits) from integer multiplies:
+// each operand is split into four words holding every fourth bit, so in any
+// partial product a column gathers at most 8 ones; the column sum then fits
+// the 4 bits up to the next column of the same class, and its low bit is the
+// XOR of the column (the "integer multiplies with holes" method, as BearSSL
+// uses for GHASH).
+R2P_HD uint64_t clmul32(uint32_t a, uint32_t b)
+{
+    const uint64_t a0 = a & 0x11111111u, a1 = a & 0x22222222u, a2 = a & 0x44444444u, a3 = a & 0x88888888u;
+    const uint64_t b0 = b & 0x11111111u, b1 = b & 0x22222222u, b2 = b & 0x44444444u, b3 = b & 0x88888888u;
+    const uint64_t z0 = (a0 * b0) ^ (a1 * b3) ^ (a2 * b2) ^ (a3 * b1);
+    const uint64_t z1 = (a0 * b1) ^ (a1 * b0) ^ (a2 * b3) ^ (a3 * b2);
+    const uint64_t z2 = (a0 * b2) ^ (a1 * b1) ^ (a2 * b0) ^ (a3 * b3);
+    const uint64_t z3 = (a0 * b3) ^ (a1 * b2) ^ (a2 * b1) ^ (a3 * b0);
+    return (z0 & 0x1111111111111111ull) | (z1 & 0x2222222222222222ull) | (z2 & 0x4444444444444444ull) |
+           (z3 & 0x8888888888888888ull);
+}
+
+// a * b mod P (reflected representation), bit by bit.
 R2P_HD uint32_t gf2_mulmod(uint32_t a, uint32_t b)
 {
     uint32_t m = 1u << 31;   // x^0
