@@ -41,7 +41,7 @@ UNIT = "MB/s"
 def workload_desc(name):
     return {
         "c1": "single 3072x3072 uint16 image (12 bits stored), DICOM window WC 2048/WW 4096 to 16-bit, "
-              "adaptive filter, LZ77 + fixed Huffman level 1 in independent blocks (config.block_size)",
+              "adaptive filter, LZ77 + fixed Huffman level 1",
         "c0": "single 512x512 uint16 CT phantom (12 bits stored), slope 1 / intercept -1024, WC 40/WW 400 to "
               "8-bit (Q15 path), adaptive filter, stored DEFLATE (level 0)",
         "c2": "single 6000x4000 RGB uint16 image, no window, adaptive filter, LZ77 + fixed Huffman level 1",
