@@ -46,7 +46,8 @@ def test_inflate_exact(engine, name, data, level):
 
 
 @pytest.mark.parametrize("level", [1, 6])
-@pytest.mark.parametrize("bs", [1024, 4096, 32752, 65520])
+# 21760 / 21776 and 32768 / 32784 straddle the LZ77 launch's change of CTA size
+@pytest.mark.parametrize("bs", [1024, 4096, 21760, 21776, 32752, 32768, 32784, 65520])
 def test_block_sizes(engine, bs, level):
     rng = np.random.default_rng(bs)
     data = np.repeat(rng.integers(0, 16, size=30000, dtype=np.uint8), 7)
