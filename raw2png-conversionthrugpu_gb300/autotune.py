@@ -8,7 +8,9 @@ on 16-bit radial-gradient images of the class's size), then checks whole
 tables on the mixed batch, and writes the table that Engine.set_tuning()
 takes.  Runs on the
 GPU; `python -m`-style entry: python raw2png-conversionthrugpu_gb300/autotune.py
-[--out path.json].
+[--out path.json].  The engine's built-in table (kDefaultTuning in
+csrc/r2p_engine.cu) repeats the committed tuning_gb300.json;
+tests/test_tuning_table.py fails when the two differ.
 """
 import json
 import os
