@@ -1,18 +1,24 @@
 """Benchmark: raw-pixel MB/s and images/s of the GB300 PNG encoder.
 
-A step is one pass of the encode path over one image of the workload.  The
-default workload is a single 3072x3072 uint16 image (12 bits stored, DICOM
-PS3.3 window WC 2048 / WW 4096 to 16-bit output, adaptive filter, LZ77 +
-fixed Huffman at level 1 in independent blocks, of the size the autotuned
-size-class table gives: config.block_size).  Eight distinct inputs are
-rotated so the working set (151 MB of raw pixels) exceeds the 129 MB L2.
+The default workload is the 3072x3072 uint16 image of the single-large-image
+configuration (12 bits stored, DICOM PS3.3 window WC 2048 / WW 4096 to 16-bit
+output, adaptive filter, LZ77 + fixed Huffman at level 1 in independent
+65520-byte blocks, the configuration's "64 KB independent blocks").  Eight
+distinct inputs (151 MB of raw pixels, more than the 129 MB L2) are encoded in
+turn; a step is one pass over the eight (eight images).
 
   value     device-resident throughput: pixels and PNG in HBM, timed with CUDA
-            events on the encode stream, max over ranks
-  e2e       the same metric through r2p_encode_png with pinned host buffers:
-            host->device pixels and device->host PNG inside the timed region
+            events on the encode streams, max over ranks
+  e2e       the same metric through r2p_encode_png_many with pinned host
+            buffers: host->device pixels and device->host PNG inside the
+            timed region
   roofline  dominant kernel: algorithmic bytes per launch / its mean duration
-            (CUDA events around each stage inside the timed region)
+            (CUDA events around each stage in a single-stream pass)
+  autotuned_blocks  the same images in the size-class table's block size
+  reference_kernels the reference's own window + filter kernels (compiled for
+            sm_103a from its sources, where the cubins were built) on the
+            same image, beside this encoder's filter stage
+  batched_c3 / served_c4  the batched and served configurations
   cpu_baseline  the oracle's CPU restatement of the reference path (window,
             filter, strip-parallel zlib level 1, PNG container) on this host
 
@@ -36,12 +42,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "raw-pixel MB/s"
 UNIT = "MB/s"
+IMAGES_PER_STEP = 8
 
 
 def workload_desc(name):
     return {
         "c1": "single 3072x3072 uint16 image (12 bits stored), DICOM window WC 2048/WW 4096 to 16-bit, "
-              "adaptive filter, LZ77 + fixed Huffman level 1",
+              "adaptive filter, LZ77 + fixed Huffman level 1 in 64 KB independent blocks",
         "c0": "single 512x512 uint16 CT phantom (12 bits stored), slope 1 / intercept -1024, WC 40/WW 400 to "
               "8-bit (Q15 path), adaptive filter, stored DEFLATE (level 0)",
         "c2": "single 6000x4000 RGB uint16 image, no window, adaptive filter, LZ77 + fixed Huffman level 1",
@@ -224,13 +231,35 @@ def measure_c3(r2p, W, eng, stream, n=1000, reps=3):
     same = bool(torch.equal(len_plain, len_batch)) and bool(torch.equal(out_plain, out_batch))
     png_bytes = int(len_batch.sum().item())
     dev_bytes = b.device_bytes
+    # roofline of the batch's dominant kernel: the same work list launched
+    # part after part on one stream with CUDA events between the stages
+    eng.set_timing(True)
+    b.launch(stream)
+    stream.sync()
+    st = eng.stage_times()
+    eng.set_timing(False)
     b.close()
+    filt_total = sum(im.filtered_bytes for im in imgs)
+    stream_total = png_bytes - 63 * n
+    alg = {"window_filter": raw_bytes + filt_total, "lz77_blocks": filt_total + stream_total,
+           "stored_blocks": 2 * filt_total, "copy_blocks": 2 * stream_total, "finalize": 0, "prepare_window": 0}
+    dname, (dms, _) = max(st.items(), key=lambda kv: kv[1][0])
+    peak, peak_kind = peaks()
+    kname = r2p.filter_kernel(imgs[0]) if dname == "window_filter" else r2p.KERNELS[r2p.STAGES.index(dname)]
+    roof = {"bound": "hbm", "kernel": kname, "achieved": round(alg[dname] / (dms / 1e3) / 1e9, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(alg[dname] / (dms / 1e3) / 1e9 / peak, 4), "peak_source": peak_kind,
+            "algorithmic_bytes": alg[dname], "ms": round(dms, 3),
+            "stage_ms": {k: round(v[0], 3) for k, v in st.items() if v[1]},
+            "stage_gbs": {k: round(alg[k] / (v[0] / 1e3) / 1e9, 1) for k, v in st.items() if v[1] and alg[k]},
+            "timing": "CUDA events between the stages of the batch's parts, launched one after another on one "
+                      "stream (the graph runs the four parts side by side)"}
     mp, mb = statistics.median(t_plain), statistics.median(t_batch)
     res = {"images": n, "raw_bytes": raw_bytes, "png_bytes": png_bytes,
            "plain_images_per_s": round(n / mp * 1e3, 1), "plain_raw_MBps": round(raw_bytes / mp / 1e3, 1),
            "batched_images_per_s": round(n / mb * 1e3, 1), "batched_raw_MBps": round(raw_bytes / mb / 1e3, 1),
            "batched_vs_plain": round(mp / mb, 2), "plain_ms": round(mp, 3), "batched_ms": round(mb, 3),
-           "kernels_per_graph": graph_launches, "batch_device_bytes": dev_bytes, "outputs_identical": same}
+           "kernels_per_graph": graph_launches, "batch_device_bytes": dev_bytes, "outputs_identical": same,
+           "roofline": roof}
     del raws, out_plain, out_batch
     torch.cuda.empty_cache()
     return res
@@ -497,14 +526,87 @@ def measure_dynamic(r2p, img, engines, streams, d_raw, nvar, steps):
             "ours_zlib_stream": len(png) - 57}
 
 
+def timed_passes(r2p, engines, streams, img, d_raw, d_png, d_len, cap, steps):
+    """`steps` passes over the rotated inputs (one image each), dealt
+    round-robin to the engines and streams, joined on the first stream;
+    device milliseconds between events around the whole region."""
+    S, nvar = len(engines), len(d_raw)
+    ev0, ev1 = r2p.Event(), r2p.Event()
+    joins = [r2p.Event() for _ in range(S)]
+    stream = streams[0]
+    ev0.record(stream)
+    for st in streams[1:]:
+        st.wait(ev0)
+    for i in range(steps * nvar):
+        s, k = i % S, i % nvar
+        engines[s].encode_png_device(img, d_raw[k].ptr, d_png[s][k].ptr, cap, d_len[s].ptr + 8 * k, streams[s])
+    for s in range(1, S):
+        joins[s].record(streams[s])
+        stream.wait(joins[s])
+    ev1.record(stream)
+    stream.sync()
+    return ev0.elapsed_ms(ev1)
+
+
+def measure_reference_kernels(r2p, img, raw, strip_rows=1024, reps=10):
+    """The reference's own window and filter kernels (src/gpu_filter.cu,
+    compiled for sm_103a from the reference sources into oracle/_ref, with
+    the reference's --use_fast_math) on the same image, launched with the
+    reference's shape per strip of `strip_rows` rows (src/gpu_filter.cu:411-434; 1024
+    rows is the modern path's default strip, include/pipeline.h:10-15):
+    device microseconds per image.  A reported baseline, only where the
+    cubins were built (they come from the reference tree)."""
+    import ctypes
+    ref = os.path.join(ROOT, "oracle", "_ref")
+    cubin = os.path.join(ref, "gpu_filter_ref_fastmath.cubin")
+    if not os.path.exists(cubin):
+        return {"unavailable": "reference cubins not built here (the reference tree is absent)"}
+    from oracle import build_oracle
+    try:
+        so = build_oracle.build_ref_gpu_runner()
+        L = ctypes.CDLL(so)
+    except (RuntimeError, OSError) as e:
+        return {"unavailable": "reference kernel runner: %s" % str(e).splitlines()[0][:200]}
+    if not hasattr(L, "rgr_time"):
+        return {"unavailable": "runner without timing entry"}
+    L.rgr_open.restype = ctypes.c_int
+    L.rgr_open.argtypes = [ctypes.c_char_p]
+    L.rgr_error.restype = ctypes.c_char_p
+    L.rgr_time.restype = ctypes.c_int
+    L.rgr_time.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                           ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                           ctypes.POINTER(ctypes.c_double)]
+    h = L.rgr_open(cubin.encode())
+    if h < 0:
+        return {"unavailable": "cubin load: %s" % L.rgr_error().decode()}
+    params = bytes(img.dicom)
+    pbuf = ctypes.create_string_buffer(params, len(params))
+    rbuf = np.ascontiguousarray(raw).view(np.uint8).reshape(-1)
+    ms_pre, ms_filt = ctypes.c_double(), ctypes.c_double()
+    # the reference windows only DICOM input (its kernel, 16-bit in and out)
+    pp = ctypes.cast(pbuf, ctypes.c_void_p) if img.window_mode == r2p.WINDOW_DICOM16 else None
+    rc = L.rgr_time(h, rbuf.ctypes.data, img.row_bytes, img.channels * img.out_bytes_per_sample, img.height, strip_rows,
+                    pp, reps, ctypes.byref(ms_pre), ctypes.byref(ms_filt))
+    if rc != 0:
+        return {"unavailable": "reference kernels: %s" % L.rgr_error().decode()}
+    tot = ms_pre.value + ms_filt.value
+    return {"kernels": "dicom_preprocess_kernel + filter_select_kernel (reference release build, --use_fast_math)",
+            "strip_rows": strip_rows, "window_us": round(ms_pre.value * 1e3, 2),
+            "filter_us": round(ms_filt.value * 1e3, 2), "total_us": round(tot * 1e3, 2),
+            "total_GBps": round((img.raw_bytes + img.filtered_bytes) / (tot / 1e3) / 1e9, 1),
+            "timing": "CUDA events around each launch, summed over the image's strips, mean of %d passes" % reps}
+
+
 def run_ours(args):
     rank, world, local, dist = dist_setup()
     import __graft_entry__ as g
     r2p = g.load_package()
     from raw2png_gb300 import workloads as W
-    nvar = 8
+    nvar = IMAGES_PER_STEP
     img, raws = make_inputs(W, args.workload, nvar)
-    # S engines on S streams, steps dealt round-robin: images on different
+    if args.workload == "c1":
+        img.block_size = 65520     # the configuration's "64 KB independent blocks"
+    # S engines on S streams, images dealt round-robin: images on different
     # streams overlap (one image alone leaves SMs idle in its LZ77 tail and
     # its per-image kernels)
     S = max(1, args.streams)
@@ -517,49 +619,33 @@ def run_ours(args):
     d_raw = [r2p.DeviceBuffer.from_array(r) for r in raws]
     d_png = [[r2p.DeviceBuffer(cap) for _ in range(nvar)] for _ in range(S)]
     d_len = [r2p.DeviceBuffer(8 * nvar) for _ in range(S)]
-    ev0, ev1 = r2p.Event(), r2p.Event()
-    ev_join = [r2p.Event() for _ in range(S)]
 
-    def step(i, s=None):
-        s = (i % S) if s is None else s
+    def one(i, s):
         k = i % nvar
         engines[s].encode_png_device(img, d_raw[k].ptr, d_png[s][k].ptr, cap, d_len[s].ptr + 8 * k, streams[s])
 
-    for i in range(max(args.warmup, S)):
-        step(i)
-    for st in streams:
-        st.sync()
+    timed_passes(r2p, engines, streams, img, d_raw, d_png, d_len, cap, max(args.warmup, 1))
     # single-stream pass: per-stage CUDA-event times for the roofline and the
-    # stage split (engine 0, the same steps, one image at a time)
+    # stage split (engine 0, one image at a time)
     eng.set_timing(True)
-    for i in range(args.steps):
-        step(i, 0)
+    for i in range(max(args.steps, nvar)):
+        one(i, 0)
     stream.sync()
     stages = eng.stage_times()
     eng.set_timing(False)
-    # timed region (device): all S streams, joined on stream 0
+    # timed region (device): `steps` passes over the eight inputs, all S streams
     clocks = ClockSampler(local)
     clocks.start()
     barrier(dist)
     stream.sync()
     launches0 = r2p.launch_count()
-    ev0.record(stream)
-    for st in streams[1:]:
-        st.wait(ev0)
-    for i in range(args.steps):
-        step(i)
-    for s in range(1, S):
-        ev_join[s].record(streams[s])
-        stream.wait(ev_join[s])
-    ev1.record(stream)
-    stream.sync()
+    ms = timed_passes(r2p, engines, streams, img, d_raw, d_png, d_len, cap, args.steps)
     barrier(dist)
     launches = r2p.launch_count() - launches0
-    ms = ev0.elapsed_ms(ev1)
     clk = clocks.stop()
     ms_max = max_over_ranks(dist, ms)
-    total_bytes = img.raw_bytes * args.steps * world
-    value = total_bytes / (ms_max / 1e3) / 1e6
+    images = args.steps * nvar
+    value = img.raw_bytes * images * world / (ms_max / 1e3) / 1e6
     # output sanity (not timed): one PNG inflates to the right size
     lens = d_len[0].download(8 * nvar).view(np.uint64)
     png = d_png[0][0].download(int(lens[0])).tobytes()
@@ -573,17 +659,33 @@ def run_ours(args):
     for lv in (0, 1, 6):
         sizes["zlib_level_%d" % lv] = len(zlib.compress(filt, lv))
     sizes["zlib_version"] = zlib.ZLIB_RUNTIME_VERSION
-    # e2e through the host entry point (r2p_encode_png) with pinned buffers:
-    # `threads` workers, each with its own engine, take steps in turn, as the
-    # reference's encode workers do; every step's pixels go host->device and
-    # its PNG device->host inside the timed region
+    if img.level == 1 and sizes["ours_zlib_stream"] >= len(filt):
+        sizes["note"] = ("fixed-Huffman LZ77 finds almost no repeats in this data: every level-1 block came out "
+                         "smaller as a stored block; levels 2-9 (dynamic Huffman) compress it")
+    # the autotuned block size (the size-class table's) on the same images
+    tuned = None
+    if img.block_size:
+        timg = type(img).from_buffer_copy(img)
+        timg.block_size = 0
+        tcap = r2p.png_bound(timg)
+        t_png = [[r2p.DeviceBuffer(tcap) for _ in range(nvar)] for _ in range(S)]
+        timed_passes(r2p, engines, streams, timg, d_raw, t_png, d_len, tcap, 1)
+        tms = timed_passes(r2p, engines, streams, timg, d_raw, t_png, d_len, tcap, args.steps)
+        tl = d_len[0].download(8 * nvar).view(np.uint64)
+        tuned = {"block_size": block_size_used(engines[0], timg), "value": round(img.raw_bytes * images / (tms / 1e3)
+                                                                                / 1e6, 2),
+                 "unit": UNIT, "ms_per_step": round(tms / args.steps, 4), "png_bytes": int(tl[0])}
+        del t_png
+    # e2e through the host entry point with pinned buffers: every image's
+    # pixels go host->device and its PNG device->host inside the timed region
     import ctypes
     import threading
     L = r2p.lib()
     e2e_api = ""
+    e2e_images = images
     if args.e2e_api == "many":
-        # one host thread, r2p_encode_png_many over all steps: up to 4 images in
-        # flight (helper engines), every step's pixels up and PNG down timed
+        # one host thread, r2p_encode_png_many over all images: up to 4 in
+        # flight (helper engines)
         pins = [r2p.PinnedBuffer(img.raw_bytes) for _ in range(2)]
         for k in range(2):
             pins[k].array[:] = raws[k].view(np.uint8).reshape(-1)
@@ -598,10 +700,9 @@ def run_ours(args):
             return lens
 
         many(2 * r2p.MANY_SLOTS)
-        e2e_steps = args.steps
         barrier(dist)
         t0 = time.perf_counter()
-        lens_e2e = many(e2e_steps)
+        lens_e2e = many(e2e_images)
         t1 = time.perf_counter()
         barrier(dist)
         assert lens_e2e[0] == comp_bytes, "e2e PNG size differs from the device-resident run"
@@ -627,8 +728,7 @@ def run_ours(args):
     if args.e2e_api == "threads":
         for t in range(T):
             e2e_run(t, 2)
-        e2e_steps = args.steps
-        share = [e2e_steps // T + (1 if t < e2e_steps % T else 0) for t in range(T)]
+        share = [e2e_images // T + (1 if t < e2e_images % T else 0) for t in range(T)]
         barrier(dist)
         t0 = time.perf_counter()
         ths = [threading.Thread(target=e2e_run, args=(t, share[t])) for t in range(T)]
@@ -642,7 +742,7 @@ def run_ours(args):
             we.close()
         e2e_api = "r2p_encode_png (pinned host buffers), %d worker thread(s), one engine each" % T
     e2e_s = max_over_ranks(dist, t1 - t0)
-    e2e_value = img.raw_bytes * e2e_steps * world / e2e_s / 1e6
+    e2e_value = img.raw_bytes * e2e_images * world / e2e_s / 1e6
     if rank != 0:
         return
     # roofline of the dominant kernel
@@ -655,30 +755,33 @@ def run_ours(args):
            "lz77_blocks": img.filtered_bytes + stream_bytes,
            "stored_blocks": img.filtered_bytes + stream_bytes,
            "copy_blocks": 2 * stream_bytes,
-           "finalize": 0, "prepare_window": 0}[dname]
-    achieved = alg / (per_launch_ms / 1e3) / 1e9
-    kname = r2p.KERNELS[r2p.STAGES.index(dname)]
+           "finalize": 0, "prepare_window": 0}
+    achieved = alg[dname] / (per_launch_ms / 1e3) / 1e9
+    kname = r2p.filter_kernel(img) if dname == "window_filter" else r2p.KERNELS[r2p.STAGES.index(dname)]
+    stage_ms = {k: round(v[0] / max(v[1], 1), 5) for k, v in stages.items() if v[1]}
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": workload_desc(args.workload), "images_per_step": 1,
-                   "l2": "%d distinct inputs rotated (%.0f MB raw > 129 MB L2)" % (nvar, nvar * img.raw_bytes / 1e6),
+        "config": {"workload": workload_desc(args.workload), "images_per_step": nvar,
+                   "step": "one pass over %d distinct inputs (%.0f MB raw > 129 MB L2)"
+                           % (nvar, nvar * img.raw_bytes / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "streams_per_gpu": S},
-        "images_per_s": round(args.steps * world / (ms_max / 1e3), 2),
+        "images_per_s": round(images * world / (ms_max / 1e3), 2),
         "png_bytes": comp_bytes,
         "compressed_vs_zlib": sizes,
-        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": img.raw_bytes,
-                "d2h_bytes_per_step": comp_bytes + 8,
-                "images_per_s": round(e2e_steps * world / e2e_s, 2),
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": img.raw_bytes * nvar,
+                "d2h_bytes_per_step": (comp_bytes + 8) * nvar,
+                "images_per_s": round(e2e_images * world / e2e_s, 2),
                 "api": e2e_api},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": round(per_launch_ms, 5),
-                     "timing": "CUDA events around each launch, single-stream pass over the same steps",
+                     "algorithmic_bytes_per_launch": alg[dname], "ms_per_launch": round(per_launch_ms, 5),
+                     "timing": "CUDA events around each launch, single-stream pass over the same images",
                      "traffic": ncu_traffic(kname, args.workload)},
-        "stages_ms_per_step": {k: round(v[0] / max(v[1], 1), 5) for k, v in stages.items() if v[1]},
+        "stages_ms_per_image": stage_ms,
+        "stages_GBps": {k: round(alg[k] / (v / 1e3) / 1e9, 1) for k, v in stage_ms.items() if alg.get(k)},
         "clocks": clk,
         "gpu_launches": launches,
     }
@@ -686,12 +789,18 @@ def run_ours(args):
     if issue is not None:
         line["roofline"]["issue_active"] = issue
         line["roofline"]["issue_note"] = ("fraction of cycles the kernel's schedulers issued an instruction "
-                                          "(ncu, profiles/ncu_traffic.md): the kernel is bound by instruction "
-                                          "issue, with DRAM traffic equal to its input once")
+                                          "(ncu, profiles/ncu_traffic.md)")
     line["config"]["tuning"] = tuning
     line["config"]["block_size"] = block_size_used(engines[0], img)
+    if tuned:
+        line["autotuned_blocks"] = tuned
     if args.workload in ("c1", "c2"):
-        line["dynamic_huffman"] = measure_dynamic(r2p, img, engines, streams, d_raw, nvar, min(args.steps, 300))
+        line["dynamic_huffman"] = measure_dynamic(r2p, img, engines, streams, d_raw, nvar,
+                                                  min(args.steps * nvar, 300))
+        line["reference_kernels"] = measure_reference_kernels(r2p, img, raws[0])
+        if "total_us" in line["reference_kernels"] and "window_filter" in stage_ms:
+            line["reference_kernels"]["ours_window_filter_us"] = round(stage_ms["window_filter"] * 1e3, 2)
+            line["reference_kernels"]["ours_kernel"] = r2p.filter_kernel(img)
     if not args.no_batched:
         line["batched_c3"] = measure_c3(r2p, W, eng, stream)
         line["served_c4"] = measure_c4(r2p, W, slots=args.server_slots)
@@ -723,7 +832,7 @@ def run_c3(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c3", "c4"])

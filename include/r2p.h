@@ -341,12 +341,13 @@ int  r2p_event_destroy(void* ev);
 int  r2p_event_record(void* ev, void* stream);
 int  r2p_event_elapsed_ms(void* ev_start, void* ev_end, float* ms);
 int  r2p_stream_wait_event(void* stream, void* ev);   /* later work on stream waits for ev */
-/* Stage timing: when enabled, each encode call records CUDA events on its
- * stream between its kernel launches; r2p_engine_stage_times() waits for
+/* Stage timing: when enabled, each encode call (and each part of an
+ * r2p_batch_launch of a batch created on the engine) records CUDA events on
+ * its stream between its kernel launches; r2p_engine_stage_times() waits for
  * them, returns per-stage device milliseconds summed over the calls since the
  * last query (and how many launches each sum covers), and resets. */
-#define R2P_STAGE_PREPARE  0   /* k_prepare_window: window tables */
-#define R2P_STAGE_FILTER   1   /* k_window_filter: window + adaptive filter */
+#define R2P_STAGE_PREPARE  0   /* k_prepare_window: window tables (shared-memory filter, BMP) */
+#define R2P_STAGE_FILTER   1   /* k_window_filter / k_window_filter_reg: window + adaptive filter */
 #define R2P_STAGE_STORED   2   /* k_stored_blocks: level-0 DEFLATE */
 #define R2P_STAGE_LZ77     3   /* k_lz77_blocks (level 1) and k_rle_dyn_blocks (2..9) */
 #define R2P_STAGE_FINALIZE 4   /* k_finalize: checksums + PNG chunks */

@@ -34,13 +34,6 @@ namespace r2p {
 
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
-// a graph replay launches the captured kernels again
-static void note_launch_graph(bool stored, bool lz, bool dyn)
-{
-    // prepare, filter, finalize; stored; LZ77; dynamic; the block copy after either
-    const uint32_t n = 3u + (stored ? 1u : 0u) + (lz ? 1u : 0u) + (dyn ? 1u : 0u) + ((lz || dyn) ? 1u : 0u);
-    g_launches.fetch_add(n, std::memory_order_relaxed);
-}
 
 static thread_local std::string t_last_error;
 
@@ -93,6 +86,9 @@ struct ImgPlan {
     int lreg = 0;      // worst-case LUT region
     int band_rows = 0; // rows per filter work item (0 = about 64 KB of filtered output)
     int hash_bits = 10;
+    bool reg = false;  // rows fit the register-resident filter kernel (k_filter_reg.cu)
+    int reg_w = 0;     // its warps per row
+    int reg_lut = 0;   // its worst-case window table bytes
 };
 
 // Built-in size-class table: the autotuner's result on GB300 (tuning_gb300.json,
@@ -193,6 +189,9 @@ static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip,
     ip.lreg = filter_lut_region(mode_guess, entries, esize);
     ip.smem = filter_smem_bytes(d.rb, d.in_pitch, mode_guess, entries, esize);
     if (ip.smem < 0) return set_err(R2P_EINVAL, "row too wide for the filter kernel");
+    ip.reg_lut = entries * esize;
+    ip.reg = reg_filter_eligible(d.rb, d.in_pitch, ip.reg_lut);
+    ip.reg_w = reg_filter_warps(d.rb);
     ip.png_bound = (uint64_t)d.prefix + F + (uint64_t)kStoredHdr * nb + (out_kind == 0 ? kPngSuffix : 4);
     if (F >= (1ull << 32) || ip.png_bound >= (1ull << 31) - 64)
         return set_err(R2P_EINVAL, "image too large for a single IDAT chunk");
@@ -382,13 +381,16 @@ static int ensure_stage(r2p_engine* e, size_t need, int* slot)
 
 // One call's work list and memory layout.
 struct Prepared {
-    std::vector<BandItem> items;
+    std::vector<BandItem> items;       // bands of the shared-memory filter kernel
+    std::vector<BandItem> ritems;      // bands of the register-resident filter kernel
     std::vector<BlockOut> blocks;
     int smem = 0, slots_total = 0, max_block = 0;
+    int rnw = 0, rsmem = 0, rslots = 0;   // register kernel: warps per CTA, shared memory, CTA slots
     uint32_t nblk = 0;
     bool any_lz = false, any_stored = false, any_dyn = false;
     uint64_t slot = 0;
-    size_t o_img = 0, o_items = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0, o_extra = 0;
+    size_t o_img = 0, o_items = 0, o_ritems = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0,
+           o_extra = 0;
     size_t total = 0;
     int hash_bits = 10;
     int stage_slot = 0;
@@ -400,9 +402,53 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
                       Prepared& P)
 {
     const int n = (int)plans.size();
-    for (auto& p : plans) P.smem = std::max(P.smem, p.smem);
+    // images whose rows fit the register-resident kernel (and whose pixels a
+    // bulk copy may read: 16-byte aligned) go there, the rest to the
+    // shared-memory kernel
+    std::vector<char> use_reg((size_t)n, 0);
+    int max_w = 0, nreg = 0;
+    for (int i = 0; i < n; i++) {
+        use_reg[(size_t)i] = plans[i].reg && plans[i].smem > 0 && i < (int)cb.raw.size() &&
+                             (reinterpret_cast<uintptr_t>(cb.raw[i]) & 15) == 0;
+        if (use_reg[(size_t)i]) {
+            max_w = std::max(max_w, plans[i].reg_w);
+            nreg++;
+        } else {
+            P.smem = std::max(P.smem, plans[i].smem);
+        }
+    }
     const int cps = P.smem > 0 ? filter_ctas_per_sm(P.smem) : 1;
     P.slots_total = e->nsm * cps;
+    if (nreg) {
+        P.rnw = reg_filter_cta_warps(max_w);
+        for (int i = 0; i < n; i++)
+            if (use_reg[(size_t)i])
+                P.rsmem = std::max(P.rsmem, reg_filter_smem(plans[i].di.rb, plans[i].di.in_pitch, plans[i].reg_lut,
+                                                             P.rnw));
+        P.rslots = e->nsm * reg_filter_ctas_per_sm(P.rnw, P.rsmem);
+        // Bands of about 64 KB of filtered output (a property of the image
+        // alone), or, when that leaves CTA slots idle, each image split evenly
+        // over the slots; a CTA's band is cut into one run of rows per group
+        // of warps, at least two rows each.
+        auto reg_bands = [&](bool spread) {
+            P.ritems.clear();
+            for (int i = 0; i < n; i++) {
+                if (!use_reg[(size_t)i]) continue;
+                const DevImage& d = plans[i].di;
+                const uint64_t G = (uint64_t)(P.rnw / plans[i].reg_w);
+                uint64_t rows = std::max<uint64_t>(2 * G, (64 * 1024 + d.rb) / ((uint64_t)d.rb + 1));
+                if (spread) {
+                    const uint64_t share = std::max<uint64_t>(1, (uint64_t)P.rslots / (uint64_t)nreg + (nreg > 1));
+                    rows = std::max<uint64_t>(2 * G, (d.height + share - 1) / share);
+                }
+                for (uint64_t r = 0; r < d.height; r += rows)
+                    P.ritems.push_back(BandItem{(uint32_t)i, (uint32_t)r,
+                                                (uint32_t)std::min<uint64_t>(d.height, r + rows)});
+            }
+        };
+        reg_bands(false);
+        if (P.ritems.size() < (size_t)P.rslots) reg_bands(true);
+    }
     uint64_t lut_total = 0, filt_total = 0;
     bool any10 = false;
     // Row bands of the filter stage.  Batches use the tuned band height of
@@ -415,6 +461,7 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
         P.items.clear();
         if (P.smem <= 0) return;
         for (int i = 0; i < n; i++) {
+            if (use_reg[(size_t)i]) continue;
             const DevImage& d = plans[i].di;
             const int T = filter_tile_rows(d.rb, d.in_pitch, P.smem, plans[i].lreg);
             const uint64_t ntiles = (d.height + T - 1) / T;
@@ -465,6 +512,7 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
     Layout L;
     P.o_img = L.take(sizeof(DevImage) * n);
     P.o_items = L.take(sizeof(BandItem) * std::max<size_t>(1, P.items.size()));
+    P.o_ritems = L.take(sizeof(BandItem) * std::max<size_t>(1, P.ritems.size()));
     P.o_blocks = L.take(sizeof(BlockOut) * std::max<size_t>(1, P.blocks.size()));
     P.desc_bytes = L.off;
     P.o_lut = L.take(lut_total);
@@ -501,6 +549,7 @@ static void write_descriptors(uint8_t* H, const std::vector<ImgPlan>& plans, con
 {
     for (size_t i = 0; i < plans.size(); i++) memcpy(H + P.o_img + i * sizeof(DevImage), &plans[i].di, sizeof(DevImage));
     if (!P.items.empty()) memcpy(H + P.o_items, P.items.data(), P.items.size() * sizeof(BandItem));
+    if (!P.ritems.empty()) memcpy(H + P.o_ritems, P.ritems.data(), P.ritems.size() * sizeof(BandItem));
     if (!P.blocks.empty()) memcpy(H + P.o_blocks, P.blocks.data(), P.blocks.size() * sizeof(BlockOut));
 }
 
@@ -519,12 +568,21 @@ static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, in
         return cudaEventRecord(tev[k], s);
     };
     const bool filt = (stages & ST_FILTER) != 0, defl = (stages & ST_DEFLATE) != 0, bmp = (stages & ST_BMP) != 0;
+    const bool old_filt = filt && !P.items.empty(), reg_filt = filt && !P.ritems.empty();
     R2P_CU(mark(0, false), "event");
-    if (filt || bmp) R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
-    R2P_CU(mark(1, filt || bmp), "event");
-    if (filt) {
+    // window tables in HBM: only the shared-memory filter kernel and the BMP
+    // export read them (the register kernel builds its table per CTA)
+    if (old_filt || bmp) R2P_CU(launch_prepare_window(dimg, n, s), "k_prepare_window");
+    R2P_CU(mark(1, old_filt || bmp), "event");
+    if (old_filt) {
         const int grid = (int)std::min<size_t>(P.items.size(), (size_t)P.slots_total);
         R2P_CU(launch_window_filter(dimg, ditems, (int)P.items.size(), grid, P.smem, s), "k_window_filter");
+    }
+    if (reg_filt) {
+        BandItem* dritems = reinterpret_cast<BandItem*>(A + P.o_ritems);
+        const int grid = (int)std::min<size_t>(P.ritems.size(), (size_t)P.rslots);
+        R2P_CU(launch_window_filter_reg(dimg, dritems, (int)P.ritems.size(), grid, P.rnw, P.rsmem, s),
+               "k_window_filter_reg");
     }
     if (bmp) R2P_CU(launch_bmp(dimg, n, P.bmp_words, e->nsm, s), "k_bmp_file");   // timed in the filter's slot
     R2P_CU(mark(2, filt || bmp), "event");
@@ -548,6 +606,15 @@ static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, in
     return R2P_OK;
 }
 
+// A graph replay launches the captured kernels of a whole encode again.
+static void note_launch_graph(const Prepared& P)
+{
+    const bool lz = P.any_lz, dyn = P.any_dyn;
+    const uint32_t n = (P.items.empty() ? 0u : 2u) + (P.ritems.empty() ? 0u : 1u) + 1u /* finalize */ +
+                       (P.any_stored ? 1u : 0u) + (lz ? 1u : 0u) + (dyn ? 1u : 0u) + ((lz || dyn) ? 1u : 0u);
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+
 // Plan into the engine arena, make sure it and the staging area are large
 // enough, and order this call after the previous one on `s`.  *extra
 // receives extra_bytes of arena space for the caller.
@@ -561,6 +628,26 @@ static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers
     if (rc) return rc;
     if (e->have_done) R2P_CU(cudaStreamWaitEvent(s, e->done, 0), "order calls");
     if (extra) *extra = e->arena + P.o_extra;
+    return R2P_OK;
+}
+
+// With stage timing on, the next record of R2P_STAGE_COUNT + 1 events (and
+// its stage mask) for one launch of the stages; nothing when timing is off.
+static int timing_slot(r2p_engine* e, cudaEvent_t** tev, uint32_t** tmask)
+{
+    *tev = nullptr;
+    *tmask = nullptr;
+    if (!e->timing) return R2P_OK;
+    if (e->tused == e->trec.size()) {
+        std::vector<cudaEvent_t> v(R2P_STAGE_COUNT + 1);
+        for (auto& ev : v) R2P_CU(cudaEventCreate(&ev), "cudaEventCreate");
+        e->trec.push_back(v);
+        e->tmask.push_back(0);
+    }
+    *tev = e->trec[e->tused].data();
+    e->tmask[e->tused] = 0;
+    *tmask = &e->tmask[e->tused];
+    e->tused++;
     return R2P_OK;
 }
 
@@ -579,19 +666,9 @@ static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers&
     e->stage_idx = (k + 1) % r2p_engine::kStageRing;
     cudaEvent_t* tev = nullptr;
     uint32_t* tmask = nullptr;
-    if (e->timing) {
-        if (e->tused == e->trec.size()) {
-            std::vector<cudaEvent_t> v(R2P_STAGE_COUNT + 1);
-            for (auto& ev : v) R2P_CU(cudaEventCreate(&ev), "cudaEventCreate");
-            e->trec.push_back(v);
-            e->tmask.push_back(0);
-        }
-        tev = e->trec[e->tused].data();
-        e->tmask[e->tused] = 0;
-        tmask = &e->tmask[e->tused];
-        e->tused++;
-    }
-    int rc = launch_stages(e, n, P, A, stages, s, tev, tmask);
+    int rc = timing_slot(e, &tev, &tmask);
+    if (rc) return rc;
+    rc = launch_stages(e, n, P, A, stages, s, tev, tmask);
     if (rc) return rc;
     R2P_CU(cudaEventRecord(e->done, s), "event");
     e->have_done = true;
@@ -1327,9 +1404,15 @@ int r2p_batch_launch(r2p_batch* b, void* stream)
     if (!b) return set_err(R2P_EINVAL, "NULL batch");
     int rc = bind(b->eng);
     if (rc) return rc;
+    // parts one after another on the stream; with the engine's stage timing
+    // on, each part's stages are timed like an encode call's
     for (BatchPart& pt : b->parts) {
+        cudaEvent_t* tev = nullptr;
+        uint32_t* tmask = nullptr;
+        rc = timing_slot(b->eng, &tev, &tmask);
+        if (rc) return rc;
         rc = launch_stages(b->eng, (int)pt.plans.size(), pt.P, b->mem + pt.off, ST_ALL,
-                           static_cast<cudaStream_t>(stream), nullptr, nullptr);
+                           static_cast<cudaStream_t>(stream), tev, tmask);
         if (rc) return rc;
     }
     return R2P_OK;
@@ -1394,7 +1477,7 @@ int r2p_batch_launch_graph(r2p_batch* b, void* stream)
         if (rc) return rc;
     }
     R2P_CU(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
-    for (const BatchPart& pt : b->parts) note_launch_graph(pt.P.any_stored, pt.P.any_lz, pt.P.any_dyn);
+    for (const BatchPart& pt : b->parts) note_launch_graph(pt.P);
     return R2P_OK;
 }
 

@@ -23,6 +23,15 @@ int filter_tile_rows(int rb, int in_pitch, int smem, int lut_region);
 int filter_lut_region(int mode, int lut_entries, int lut_esize);
 int filter_ctas_per_sm(int smem);
 
+// k_filter_reg.cu: rows of up to 8 KB held in registers by groups of warps
+int reg_filter_warps(int rb);
+bool reg_filter_eligible(int rb, int in_pitch, int lut_bytes);
+int reg_filter_cta_warps(int max_w);
+int reg_filter_smem(int rb, int in_pitch, int lut_bytes, int nw);
+int reg_filter_ctas_per_sm(int nw, int smem);
+cudaError_t launch_window_filter_reg(DevImage* imgs, const BandItem* items, int nitems, int grid, int nw, int smem,
+                                     cudaStream_t s);
+
 // k_deflate.cu
 int stored_smem_bytes(int block_size);
 cudaError_t launch_stored(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block,
