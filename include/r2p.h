@@ -218,8 +218,10 @@ int r2p_deflate_raw_device(r2p_engine* eng, const void* d_in, size_t len, int le
  * exit, so len is limited to 1 MiB (1048576 bytes); larger inputs are
  * rejected with R2P_EINVAL.  The first call on a device sets the array up
  * (looks up its address, builds the power table and waits for it): make that
- * call before any stream capture.  All calls share the array, so calls that
- * overlap on the GPU race: issue them on one stream or order them.  Output is
+ * call before any stream capture.  That set-up lasts for the process: after
+ * cudaDeviceReset the entry point must not be called again.  All calls share
+ * the array, so calls that overlap on the GPU race: issue them on one stream
+ * or order them.  Output is
  * byte-identical to r2p_zlib_compress_device for the same input, level and
  * block_size. */
 int r2p_zlib_compress_noalloc(const void* d_in, size_t len, int level, int block_size,

@@ -22,7 +22,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+# the reference tree: R2P_REFERENCE_DIR, or --reference DIR on the command
+# line, else the location this build's container mounts it at
+REF = os.environ.get("R2P_REFERENCE_DIR", "/root/reference")
 REF_DIR = os.path.join(HERE, "_ref")
 
 
@@ -117,5 +119,7 @@ def build_ref_gpu_runner(verbose=False):
 
 if __name__ == "__main__":
     v = "-v" in sys.argv
+    if "--reference" in sys.argv:
+        REF = sys.argv[sys.argv.index("--reference") + 1]
     print(build_oracle(v))
     print("reference harness built:", build_ref(v))

@@ -16,8 +16,9 @@
 //                        is_last on the final strip, writer order)
 // The zlib calls are the reference's own third-party dependency (zlib 1.3 on
 // both build machines), so for equal inputs this port emits the same bytes as
-// the reference build; tests/test_oracle_ref.py checks that byte equality
-// against the reference's own sources compiled into oracle/_ref.
+// the reference build; tests/test_oracle.py::test_port_png_matches_reference_bytes
+// checks that byte equality against the reference's own sources compiled into
+// oracle/_ref.
 #include <zlib.h>
 
 #include <algorithm>

@@ -370,8 +370,10 @@ __device__ __forceinline__ void group_sync(int id, int nthreads)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// Time limit for one bulk copy of a tile to land in shared memory.
+// Time limit for one bulk copy of a tile to land in shared memory, and the
+// further wait for it after a timeout before the CTA gives its memory back.
 constexpr uint64_t kBulkWaitNs = 200ull * 1000 * 1000;
+constexpr uint64_t kBulkDrainNs = 2000ull * 1000 * 1000;
 
 __global__ void __launch_bounds__(kFiltThreads)
 k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items, int nitems, int smem_bytes)
@@ -443,11 +445,13 @@ k_window_filter(DevImage* __restrict__ imgs, const BandItem* __restrict__ items,
             if (bulk) {
                 const bool ok = mbar_wait_bounded(&bar, phase, kBulkWaitNs);
                 if (__syncthreads_or(!ok)) {
-                    // the copy did not land in time: report, give it one more
-                    // bounded wait, and leave this kernel
+                    // the copy did not land in time: report it, and keep the
+                    // CTA (and its shared memory) until the copy has landed,
+                    // for up to kBulkDrainNs more; only a copy engine that
+                    // stopped answering altogether outlasts that
                     if (tid == 0) {
                         atomicExch(&d.status, R2P_ETIMEOUT);
-                        mbar_wait_bounded(&bar, phase, kBulkWaitNs);
+                        mbar_wait_bounded(&bar, phase, kBulkDrainNs);
                     }
                     __syncthreads();
                     return;

@@ -1,12 +1,17 @@
-// r2p_engine.cu -- host side of the encoder: the C ABI of include/r2p.h.
+// r2p_engine.cu -- host side of the encoder: the C ABI of include/r2p.h for
+// engines, planning and the per-call encodes (batches: r2p_batch.cu; the
+// request server: r2p_server.cu; shared internals: r2p_engine_impl.h).
 //
 // An engine owns one device's scratch memory (a reusable arena), a pinned
 // staging area for work descriptors, and the CRC power table.  Every encode
 // call builds a plan on the host (per image: geometry, window request, row
 // bands for the filter kernel, DEFLATE blocks), uploads it in one copy, and
 // launches one kernel per stage over the whole work list:
-//   k_prepare_window -> k_window_filter -> k_stored_blocks | k_lz77_blocks
-//   -> k_finalize -> (k_copy_blocks)
+//   [k_prepare_window ->] k_window_filter_reg | k_window_filter
+//   -> k_stored_blocks | k_lz77_blocks | k_rle_dyn_blocks -> k_finalize
+//   -> (k_copy_blocks)
+// (k_prepare_window builds window tables in HBM for the shared-memory filter
+// kernel and the BMP export; the register-resident kernel builds its own.)
 // Calls are ordered through the engine: each call waits (on the device, not
 // the host) for the previous call's last kernel before reusing the arena.
 #include <cuda_runtime.h>
@@ -26,9 +31,7 @@
 #include <unordered_map>
 #include <vector>
 
-#include "r2p_common.h"
-#include "r2p_device.h"
-#include "r2p_kernels.h"
+#include "r2p_engine_impl.h"
 
 namespace r2p {
 
@@ -37,13 +40,13 @@ void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static thread_local std::string t_last_error;
 
-static int set_err(int code, const char* what)
+int set_err(int code, const char* what)
 {
     t_last_error = what ? what : "";
     return code;
 }
 
-static int cuda_err(cudaError_t e, const char* where)
+int cuda_err(cudaError_t e, const char* where)
 {
     char buf[256];
     snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
@@ -51,13 +54,7 @@ static int cuda_err(cudaError_t e, const char* where)
     return e == cudaErrorMemoryAllocation ? R2P_ENOMEM : R2P_ECUDA;
 }
 
-#define R2P_CU(call, where)                                     \
-    do {                                                        \
-        cudaError_t _e = (call);                                \
-        if (_e != cudaSuccess) return cuda_err(_e, where);      \
-    } while (0)
 
-static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // x^(8 * j * 2^(10 l)) mod P, l = 0..3, j = 0..1023 (see xpow8n)
 static void build_xpow(std::vector<uint32_t>& tab)
@@ -77,25 +74,12 @@ static void build_xpow(std::vector<uint32_t>& tab)
 // ---------------------------------------------------------------------------
 // planning
 // ---------------------------------------------------------------------------
-struct ImgPlan {
-    DevImage di;
-    uint64_t raw_bytes = 0;
-    uint64_t lut_cap = 0;
-    uint64_t png_bound = 0;
-    int smem = 0;      // filter smem wanted
-    int lreg = 0;      // worst-case LUT region
-    int band_rows = 0; // rows per filter work item (0 = about 64 KB of filtered output)
-    int hash_bits = 10;
-    bool reg = false;  // rows fit the register-resident filter kernel (k_filter_reg.cu)
-    int reg_w = 0;     // its warps per row
-    int reg_lut = 0;   // its worst-case window table bytes
-};
 
 // Built-in size-class table: the autotuner's result on GB300 (tuning_gb300.json,
 // written by autotune.py): 21760-byte level-1 blocks in every class (three LZ77
 // CTAs per SM), filter rows per work item by class, 2^10-entry hash tables.
 // Engines may load another table.
-static const std::vector<r2p_tuning> kDefaultTuning = {{327680, 21760, 16, 10},
+const std::vector<r2p_tuning> kDefaultTuning = {{327680, 21760, 16, 10},
                                                        {1310720, 21760, 0, 10},
                                                        {6168576, 21760, 32, 10},
                                                        {14557184, 21760, 32, 10},
@@ -108,8 +92,7 @@ static const r2p_tuning& tune_for(const std::vector<r2p_tuning>& t, uint64_t raw
     return t.back();
 }
 
-static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip,
-                      const std::vector<r2p_tuning>& tune = kDefaultTuning)
+int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip, const std::vector<r2p_tuning>& tune)
 {
     if (im.width < 1 || im.height < 1) return set_err(R2P_EINVAL, "width and height must be >= 1");
     if (im.channels != 1 && im.channels != 3 && im.channels != 4)
@@ -205,7 +188,7 @@ static int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip,
 // samples by one byte (the first: big-endian data as the loaders leave it,
 // and the reference's choice for 16-bit colour DICOM too), 8-bit samples as
 // they are.
-static int plan_bmp(const r2p_image& im, ImgPlan& ip)
+int plan_bmp(const r2p_image& im, ImgPlan& ip)
 {
     if (im.width < 1 || im.height < 1) return set_err(R2P_EINVAL, "width and height must be >= 1");
     if (im.channels != 1 && im.channels != 3 && im.channels != 4)
@@ -280,125 +263,13 @@ static int plan_bmp(const r2p_image& im, ImgPlan& ip)
 
 using namespace r2p;
 
-struct r2p_engine {
-    int device = 0;
-    size_t budget = 0;
-    int nsm = 1;
-    uint32_t* d_xpow = nullptr;
-    uint8_t* arena = nullptr;
-    size_t arena_cap = 0;
-    // pinned staging ring for descriptor uploads: the host may run up to
-    // kStageRing calls ahead of the device before reusing a slot
-    static constexpr int kStageRing = 8;
-    uint8_t* h_stage[kStageRing] = {};
-    size_t stage_cap[kStageRing] = {};
-    cudaEvent_t staged[kStageRing] = {};   // upload of the call that last used the slot
-    bool stage_used[kStageRing] = {};
-    int stage_idx = 0;
-    cudaEvent_t done = nullptr;     // last kernel of the previous call
-    bool have_done = false;
-    // stream of the host-buffer entry points: engines driven from different
-    // threads overlap their copies and kernels instead of sharing the
-    // legacy default stream
-    cudaStream_t hstream = nullptr;
-    // r2p_encode_png_many: helper engines (own arena and stream each), the
-    // pinned length words they read back, and their events
-    std::vector<r2p_engine*> helpers;
-    uint64_t* many_lens = nullptr;
-    cudaEvent_t many_ev[R2P_MANY_SLOTS] = {};
-    // per slot: the PNG download runs on its own stream, so the next image's
-    // upload overlaps it; the next image's kernels wait for its event
-    cudaStream_t many_dl[R2P_MANY_SLOTS] = {};
-    cudaEvent_t many_dl_ev[R2P_MANY_SLOTS] = {};
-    std::mutex mu;
-    // stage timing (events between stage launches on the call's stream)
-    bool timing = false;
-    std::vector<std::vector<cudaEvent_t>> trec;   // per timed call: R2P_STAGE_COUNT + 1 events
-    std::vector<uint32_t> tmask;                  // stages each timed call launched
-    size_t tused = 0;
-    std::vector<r2p_tuning> tuning = kDefaultTuning;
-};
 
 
 namespace r2p {
 
-// Bump allocator over one plan's arena layout.
-struct Layout {
-    size_t off = 0;
-    size_t take(size_t bytes)
-    {
-        const size_t o = off;
-        off = align_up(off + bytes, 256);
-        return o;
-    }
-};
-
-struct CallBuffers {
-    // per image, caller-provided or arena
-    std::vector<const uint8_t*> raw;
-    std::vector<uint8_t*> filt;
-    std::vector<const uint8_t*> prior;
-    std::vector<uint8_t*> last_row;     // optional; empty = none
-    std::vector<uint8_t*> out;
-    std::vector<uint64_t> out_cap;
-    std::vector<uint64_t*> out_len;
-};
-
-enum Stages { ST_FILTER = 1, ST_DEFLATE = 2, ST_ALL = 3, ST_BMP = 4 };
-
-static int ensure_arena(r2p_engine* e, size_t need)
-{
-    if (need <= e->arena_cap) return R2P_OK;
-    if (e->budget && need > e->budget) return set_err(R2P_EBUDGET, "request exceeds the engine's HBM budget");
-    if (e->have_done) R2P_CU(cudaEventSynchronize(e->done), "arena wait");
-    if (e->arena) cudaFree(e->arena);
-    e->arena = nullptr;
-    e->arena_cap = 0;
-    size_t cap = align_up(need + need / 4, 1 << 20);
-    if (e->budget && cap > e->budget) cap = need;
-    R2P_CU(cudaMalloc(&e->arena, cap), "arena cudaMalloc");
-    e->arena_cap = cap;
-    return R2P_OK;
-}
-
-// Take the next staging slot, waiting for the upload that last used it and
-// growing it to `need` bytes.
-static int ensure_stage(r2p_engine* e, size_t need, int* slot)
-{
-    const int k = e->stage_idx;
-    if (e->stage_used[k]) R2P_CU(cudaEventSynchronize(e->staged[k]), "staging wait");
-    if (need > e->stage_cap[k]) {
-        if (e->h_stage[k]) cudaFreeHost(e->h_stage[k]);
-        e->h_stage[k] = nullptr;
-        e->stage_cap[k] = 0;
-        const size_t cap = align_up(need * 2, 1 << 16);
-        R2P_CU(cudaMallocHost(&e->h_stage[k], cap), "staging cudaMallocHost");
-        e->stage_cap[k] = cap;
-    }
-    *slot = k;
-    return R2P_OK;
-}
-
-// One call's work list and memory layout.
-struct Prepared {
-    std::vector<BandItem> items;       // bands of the shared-memory filter kernel
-    std::vector<BandItem> ritems;      // bands of the register-resident filter kernel
-    std::vector<BlockOut> blocks;
-    int smem = 0, slots_total = 0, max_block = 0;
-    int rnw = 0, rsmem = 0, rslots = 0;   // register kernel: warps per CTA, shared memory, CTA slots
-    uint32_t nblk = 0;
-    bool any_lz = false, any_stored = false, any_dyn = false;
-    uint64_t slot = 0;
-    size_t o_img = 0, o_items = 0, o_ritems = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0,
-           o_extra = 0;
-    size_t total = 0;
-    int hash_bits = 10;
-    int stage_slot = 0;
-    uint32_t bmp_words = 0;    // 4-byte words of the largest BMP file
-};
 
 // Work list and memory layout of one call (or one batch) over n images.
-static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
+void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
                       Prepared& P)
 {
     const int n = (int)plans.size();
@@ -523,7 +394,7 @@ static void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuff
 }
 
 // Point the image descriptors at their buffers inside memory base A.
-static void fill_pointers(std::vector<ImgPlan>& plans, const CallBuffers& cb, const Prepared& P, uint8_t* A)
+void fill_pointers(std::vector<ImgPlan>& plans, const CallBuffers& cb, const Prepared& P, uint8_t* A)
 {
     uint64_t lut_off = P.o_lut, filt_off = P.o_filt;
     for (size_t i = 0; i < plans.size(); i++) {
@@ -545,7 +416,7 @@ static void fill_pointers(std::vector<ImgPlan>& plans, const CallBuffers& cb, co
     }
 }
 
-static void write_descriptors(uint8_t* H, const std::vector<ImgPlan>& plans, const Prepared& P)
+void write_descriptors(uint8_t* H, const std::vector<ImgPlan>& plans, const Prepared& P)
 {
     for (size_t i = 0; i < plans.size(); i++) memcpy(H + P.o_img + i * sizeof(DevImage), &plans[i].di, sizeof(DevImage));
     if (!P.items.empty()) memcpy(H + P.o_items, P.items.data(), P.items.size() * sizeof(BandItem));
@@ -556,7 +427,7 @@ static void write_descriptors(uint8_t* H, const std::vector<ImgPlan>& plans, con
 // Launch the stage kernels over a planned, uploaded work list at base A.
 // With tmask != null, tev[k] is recorded before stage k (and tev[6] after
 // the last) and *tmask gets the stages that ran.
-static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stages, cudaStream_t s,
+int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stages, cudaStream_t s,
                          cudaEvent_t* tev, uint32_t* tmask)
 {
     DevImage* dimg = reinterpret_cast<DevImage*>(A + P.o_img);
@@ -607,7 +478,7 @@ static int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, in
 }
 
 // A graph replay launches the captured kernels of a whole encode again.
-static void note_launch_graph(const Prepared& P)
+void note_launch_graph(const Prepared& P)
 {
     const bool lz = P.any_lz, dyn = P.any_dyn;
     const uint32_t n = (P.items.empty() ? 0u : 2u) + (P.ritems.empty() ? 0u : 1u) + 1u /* finalize */ +
@@ -618,7 +489,7 @@ static void note_launch_graph(const Prepared& P)
 // Plan into the engine arena, make sure it and the staging area are large
 // enough, and order this call after the previous one on `s`.  *extra
 // receives extra_bytes of arena space for the caller.
-static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
+int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, size_t extra_bytes,
                    cudaStream_t s, Prepared& P, uint8_t** extra)
 {
     plan_work(e, plans, cb, extra_bytes, P);
@@ -633,7 +504,7 @@ static int prepare(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers
 
 // With stage timing on, the next record of R2P_STAGE_COUNT + 1 events (and
 // its stage mask) for one launch of the stages; nothing when timing is off.
-static int timing_slot(r2p_engine* e, cudaEvent_t** tev, uint32_t** tmask)
+int timing_slot(r2p_engine* e, cudaEvent_t** tev, uint32_t** tmask)
 {
     *tev = nullptr;
     *tmask = nullptr;
@@ -652,7 +523,7 @@ static int timing_slot(r2p_engine* e, cudaEvent_t** tev, uint32_t** tmask)
 }
 
 // Fill the device pointers, upload the descriptors and launch the stages.
-static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, Prepared& P, int stages,
+int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb, Prepared& P, int stages,
                   cudaStream_t s)
 {
     const int n = (int)plans.size();
@@ -675,7 +546,7 @@ static int launch(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers&
     return R2P_OK;
 }
 
-static int run(r2p_engine* e, std::vector<ImgPlan>& plans, CallBuffers& cb, int stages, cudaStream_t s)
+int run(r2p_engine* e, std::vector<ImgPlan>& plans, CallBuffers& cb, int stages, cudaStream_t s)
 {
     Prepared P;
     int rc = prepare(e, plans, cb, 0, s, P, nullptr);
@@ -683,7 +554,7 @@ static int run(r2p_engine* e, std::vector<ImgPlan>& plans, CallBuffers& cb, int 
     return launch(e, plans, cb, P, stages, s);
 }
 
-static int bind(r2p_engine* e)
+int bind(r2p_engine* e)
 {
     R2P_CU(cudaSetDevice(e->device), "cudaSetDevice");
     return R2P_OK;
@@ -691,24 +562,6 @@ static int bind(r2p_engine* e)
 
 }  // namespace r2p
 
-// One part of a batch: its own work list and memory, launched as its own
-// branch of the batch's graph.
-struct BatchPart {
-    std::vector<ImgPlan> plans;
-    CallBuffers cb;
-    Prepared P;
-    size_t off = 0;                   // of the part's descriptors + scratch in mem
-};
-
-struct r2p_batch {
-    r2p_engine* eng = nullptr;
-    int n = 0;
-    std::vector<BatchPart> parts;
-    uint8_t* mem = nullptr;           // descriptors + tables + scratch of every part, owned
-    size_t total = 0;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-};
 
 // status message hook for the other translation units of the library
 int r2p_internal_set_error(int code, const char* msg) { return r2p::set_err(code, msg); }
@@ -1327,173 +1180,6 @@ int r2p_engine_get_tuning(r2p_engine* e, int cap, r2p_tuning* out, int* n)
     return R2P_OK;
 }
 
-// Batches of at least this many images are split into kBatchParts parts
-// (size-balanced: images dealt out by decreasing size) whose stage kernels
-// run as parallel branches of one graph, so one part's stage tails overlap
-// another's work; each image's bytes do not depend on its part.
-constexpr int kBatchParts = 4;
-constexpr int kBatchSplitMin = 64;
-
-int r2p_batch_create(r2p_engine* e, int n, const r2p_image* imgs, const void* const* d_pixels, void* const* d_pngs,
-                     const size_t* png_caps, uint64_t* d_png_lens, r2p_batch** out)
-{
-    if (!e || n < 1 || !imgs || !d_pixels || !d_pngs || !png_caps || !d_png_lens || !out)
-        return set_err(R2P_EINVAL, "NULL argument");
-    *out = nullptr;
-    std::lock_guard<std::mutex> lk(e->mu);
-    int rc = bind(e);
-    if (rc) return rc;
-    std::vector<ImgPlan> all((size_t)n);
-    for (int i = 0; i < n; i++) {
-        rc = plan_image(imgs[i], 0, all[i], e->tuning);
-        if (!rc && png_caps[i] < all[i].png_bound) rc = set_err(R2P_ENOSPC, "png_cap below r2p_png_bound()");
-        if (!rc && (!d_pixels[i] || !d_pngs[i])) rc = set_err(R2P_EINVAL, "NULL buffer");
-        if (rc) return rc;
-    }
-    const int K = n >= kBatchSplitMin ? kBatchParts : 1;
-    std::vector<int> order((size_t)n);
-    for (int i = 0; i < n; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return all[x].raw_bytes > all[y].raw_bytes; });
-    r2p_batch* b = new r2p_batch();
-    b->eng = e;
-    b->n = n;
-    b->parts.resize((size_t)K);
-    for (int j = 0; j < n; j++) {
-        const int i = order[j];
-        BatchPart& pt = b->parts[(size_t)(j % K)];
-        pt.plans.push_back(all[i]);
-        pt.cb.raw.push_back(static_cast<const uint8_t*>(d_pixels[i]));
-        pt.cb.filt.push_back(nullptr);
-        pt.cb.prior.push_back(nullptr);
-        pt.cb.out.push_back(static_cast<uint8_t*>(d_pngs[i]));
-        pt.cb.out_cap.push_back(png_caps[i]);
-        pt.cb.out_len.push_back(d_png_lens + i);
-    }
-    for (BatchPart& pt : b->parts) {
-        plan_work(e, pt.plans, pt.cb, 0, pt.P);
-        pt.off = b->total;
-        b->total += align_up(pt.P.total, 256);
-    }
-    if (e->budget && b->total > e->budget) {
-        delete b;
-        return set_err(R2P_EBUDGET, "batch exceeds the engine's HBM budget");
-    }
-    cudaError_t ce = cudaMalloc(&b->mem, b->total);
-    if (ce != cudaSuccess) {
-        delete b;
-        return cuda_err(ce, "batch cudaMalloc");
-    }
-    for (BatchPart& pt : b->parts) {
-        fill_pointers(pt.plans, pt.cb, pt.P, b->mem + pt.off);
-        std::vector<uint8_t> host(pt.P.desc_bytes);
-        write_descriptors(host.data(), pt.plans, pt.P);
-        ce = cudaMemcpy(b->mem + pt.off, host.data(), pt.P.desc_bytes, cudaMemcpyHostToDevice);
-        if (ce != cudaSuccess) {
-            cudaFree(b->mem);
-            delete b;
-            return cuda_err(ce, "batch descriptor upload");
-        }
-    }
-    *out = b;
-    return R2P_OK;
-}
-
-int r2p_batch_launch(r2p_batch* b, void* stream)
-{
-    if (!b) return set_err(R2P_EINVAL, "NULL batch");
-    int rc = bind(b->eng);
-    if (rc) return rc;
-    // parts one after another on the stream; with the engine's stage timing
-    // on, each part's stages are timed like an encode call's
-    for (BatchPart& pt : b->parts) {
-        cudaEvent_t* tev = nullptr;
-        uint32_t* tmask = nullptr;
-        rc = timing_slot(b->eng, &tev, &tmask);
-        if (rc) return rc;
-        rc = launch_stages(b->eng, (int)pt.plans.size(), pt.P, b->mem + pt.off, ST_ALL,
-                           static_cast<cudaStream_t>(stream), tev, tmask);
-        if (rc) return rc;
-    }
-    return R2P_OK;
-}
-
-// Capture every part's stage kernels into one graph: part 0 on the capture
-// stream, the others on forked streams joined back before the capture ends.
-static int capture_batch(r2p_batch* b, cudaStream_t cs)
-{
-    const int K = (int)b->parts.size();
-    std::vector<cudaStream_t> fs((size_t)K, nullptr);
-    std::vector<cudaEvent_t> ev((size_t)K, nullptr);
-    int rc = R2P_OK;
-    cudaError_t ce = cudaSuccess;
-    for (int k = 0; k < K && ce == cudaSuccess; k++) {
-        ce = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
-        if (ce == cudaSuccess && k > 0) ce = cudaStreamCreateWithFlags(&fs[k], cudaStreamNonBlocking);
-    }
-    if (ce == cudaSuccess) ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (ce == cudaSuccess) {
-        fs[0] = cs;
-        if (K > 1) ce = cudaEventRecord(ev[0], cs);
-        for (int k = 1; k < K && ce == cudaSuccess; k++) ce = cudaStreamWaitEvent(fs[k], ev[0], 0);
-        for (int k = 0; k < K && ce == cudaSuccess && !rc; k++)
-            rc = launch_stages(b->eng, (int)b->parts[k].plans.size(), b->parts[k].P, b->mem + b->parts[k].off,
-                               ST_ALL, fs[k], nullptr, nullptr);
-        for (int k = 1; k < K && ce == cudaSuccess && !rc; k++) {
-            ce = cudaEventRecord(ev[k], fs[k]);
-            if (ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, ev[k], 0);
-        }
-        cudaGraph_t g = nullptr;
-        const cudaError_t ce2 = cudaStreamEndCapture(cs, &g);
-        if (ce == cudaSuccess) ce = ce2;
-        if (!rc && ce == cudaSuccess) {
-            b->graph = g;
-            ce = cudaGraphInstantiate(&b->exec, g, 0);
-        } else if (g) {
-            cudaGraphDestroy(g);
-        }
-    }
-    for (int k = 1; k < K; k++)
-        if (fs[k]) cudaStreamDestroy(fs[k]);
-    for (auto x : ev)
-        if (x) cudaEventDestroy(x);
-    if (rc) return rc;
-    if (ce != cudaSuccess) return cuda_err(ce, "graph capture");
-    return R2P_OK;
-}
-
-int r2p_batch_launch_graph(r2p_batch* b, void* stream)
-{
-    if (!b) return set_err(R2P_EINVAL, "NULL batch");
-    int rc = bind(b->eng);
-    if (rc) return rc;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (!b->exec) {
-        // capture on a private stream so the caller's stream state is untouched
-        cudaStream_t cs;
-        R2P_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
-        rc = capture_batch(b, cs);
-        cudaStreamDestroy(cs);
-        if (rc) return rc;
-    }
-    R2P_CU(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
-    for (const BatchPart& pt : b->parts) note_launch_graph(pt.P);
-    return R2P_OK;
-}
-
-size_t r2p_batch_device_bytes(const r2p_batch* b) { return b ? b->total : 0; }
-
-void r2p_batch_destroy(r2p_batch* b)
-{
-    if (!b) return;
-    cudaSetDevice(b->eng->device);
-    cudaDeviceSynchronize();
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->mem) cudaFree(b->mem);
-    delete b;
-}
-
 uint32_t r2p_crc32_combine(uint32_t crc1, uint32_t crc2, uint64_t len2)
 {
     static CrcPow pw = [] { CrcPow t; crc_init_pow(t); return t; }();
@@ -1585,600 +1271,3 @@ int r2p_event_elapsed_ms(void* a, void* b, float* ms)
 
 }  // extern "C"
 
-
-// ===========================================================================
-// Serving: continuous batching over pooled device memory
-// ===========================================================================
-namespace r2p {
-
-// First-fit allocator over [0, cap) in 256-byte units with coalescing frees.
-class RangeAllocator {
-public:
-    void init(size_t cap)
-    {
-        free_.clear();
-        cap_ = cap;
-        used_ = 0;
-        if (cap) free_[0] = cap;
-    }
-    bool alloc(size_t n, size_t& off)
-    {
-        n = align_up(n ? n : 1, 256);
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < n) continue;
-            off = it->first;
-            const size_t rest = it->second - n, o2 = it->first + n;
-            free_.erase(it);
-            if (rest) free_[o2] = rest;
-            used_ += n;
-            peak_ = std::max(peak_, used_);
-            return true;
-        }
-        return false;
-    }
-    void release(size_t off, size_t n)
-    {
-        n = align_up(n ? n : 1, 256);
-        used_ -= n;
-        auto it = free_.emplace(off, n).first;
-        auto nx = std::next(it);
-        if (nx != free_.end() && it->first + it->second == nx->first) {
-            it->second += nx->second;
-            free_.erase(nx);
-        }
-        if (it != free_.begin()) {
-            auto pv = std::prev(it);
-            if (pv->first + pv->second == it->first) {
-                pv->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-    size_t used() const { return used_; }
-    size_t peak() const { return peak_; }
-    size_t cap() const { return cap_; }
-
-private:
-    std::map<size_t, size_t> free_;
-    size_t cap_ = 0, used_ = 0, peak_ = 0;
-};
-
-using Clock = std::chrono::steady_clock;
-
-enum ReqState { RQ_PENDING, RQ_RUNNING, RQ_DONE, RQ_FAILED, RQ_CANCELED };
-
-struct Request {
-    uint64_t ticket = 0;
-    r2p_image img{};
-    ImgPlan plan;
-    size_t raw_bytes = 0, bound = 0, est_scratch = 0;
-    // host side: pixels then PNG, in the pinned pool or (when full) in `heap`
-    size_t h_off = 0, h_bytes = 0;
-    bool h_pinned = false;
-    std::vector<uint8_t> heap;
-    uint8_t* h_px = nullptr;
-    uint8_t* h_png = nullptr;
-    // device side: pixels then PNG
-    size_t d_off = 0, d_bytes = 0;
-    int state = RQ_PENDING;
-    int status = R2P_OK;
-    size_t png_len = 0;
-    Clock::time_point t_submit, t_dispatch, t_done;
-};
-
-struct Slot {
-    cudaStream_t s = nullptr;
-    bool active = false;
-    int phase = 0;                 // 1: kernels + lengths queued, 2: PNG copies queued
-    // set by the stream's host functions, which never take the server mutex
-    std::atomic<bool> lens_ready{false}, pngs_ready{false};
-    std::vector<Request*> reqs;
-    std::vector<ImgPlan> plans;
-    Prepared P;
-    size_t scratch_off = 0, scratch_bytes = 0;
-    // descriptor + length staging: a range of the pinned pool, else `heap`
-    size_t stage_off = 0, stage_bytes = 0;
-    bool stage_pinned = false;
-    std::vector<uint8_t> heap;
-    uint8_t* h_desc = nullptr;
-    uint64_t* h_lens = nullptr;
-    void* srv = nullptr;           // the owning r2p_server
-};
-
-}  // namespace r2p
-
-// Locking: `mu` guards the queues, the pools, request states and statistics.
-// The dispatcher makes its CUDA calls without `mu` where it can, and the
-// stream host functions take only `wake_mu` (never held across a CUDA call),
-// so a CUDA call that waits for the device can never wait on a host function
-// that waits on a lock.
-struct r2p_server {
-    r2p_engine* eng = nullptr;
-    r2p_server_config cfg{};
-    uint8_t* dmem = nullptr;
-    uint8_t* hmem = nullptr;
-    r2p::RangeAllocator dpool, hpool;
-    std::mutex mu;
-    std::condition_variable cv_done;
-    std::mutex wake_mu;
-    std::condition_variable cv_wake;
-    uint64_t wake_seq = 0;
-    std::deque<r2p::Request*> pending;
-    std::unordered_map<uint64_t, r2p::Request*> reqs;
-    std::vector<std::unique_ptr<r2p::Slot>> slots;
-    std::thread dispatcher;
-    bool stop = false;
-    uint64_t next_ticket = 1;
-    // statistics
-    std::vector<double> lat_ms;
-    uint64_t completed = 0, failed = 0, canceled = 0, batches = 0, batched_images = 0;
-    int dispatch_error = R2P_OK;
-};
-
-namespace r2p {
-
-static void wake_dispatcher(r2p_server* sv)
-{
-    {
-        std::lock_guard<std::mutex> lk(sv->wake_mu);
-        sv->wake_seq++;
-    }
-    sv->cv_wake.notify_one();
-}
-
-static uint64_t wake_snapshot(r2p_server* sv)
-{
-    std::lock_guard<std::mutex> lk(sv->wake_mu);
-    return sv->wake_seq;
-}
-
-static void CUDART_CB host_lens_ready(void* p)
-{
-    Slot* sl = static_cast<Slot*>(p);
-    sl->lens_ready.store(true, std::memory_order_release);
-    wake_dispatcher(reinterpret_cast<r2p_server*>(sl->srv));
-}
-
-static void CUDART_CB host_pngs_ready(void* p)
-{
-    Slot* sl = static_cast<Slot*>(p);
-    sl->pngs_ready.store(true, std::memory_order_release);
-    wake_dispatcher(reinterpret_cast<r2p_server*>(sl->srv));
-}
-
-static double ms_between(Clock::time_point a, Clock::time_point b)
-{
-    return std::chrono::duration<double, std::milli>(b - a).count();
-}
-
-// Finish a request (mu held): free its device memory and count it.
-static void finish_request(r2p_server* sv, Request* r, int state, int status)
-{
-    if (r->d_bytes) sv->dpool.release(r->d_off, r->d_bytes);
-    r->d_bytes = 0;
-    r->state = state;
-    r->status = status;
-    r->t_done = Clock::now();
-    if (state == RQ_DONE) {
-        sv->completed++;
-        sv->lat_ms.push_back(ms_between(r->t_submit, r->t_done));
-    } else if (state == RQ_FAILED) {
-        sv->failed++;
-    } else {
-        sv->canceled++;
-    }
-}
-
-// Release a slot's scratch and staging (mu held).
-static void release_slot_memory(r2p_server* sv, Slot& sl)
-{
-    if (sl.scratch_bytes) sv->dpool.release(sl.scratch_off, sl.scratch_bytes);
-    if (sl.stage_pinned) sv->hpool.release(sl.stage_off, sl.stage_bytes);
-    sl.scratch_bytes = sl.stage_bytes = 0;
-    sl.stage_pinned = false;
-}
-
-// Phase 1 -> 2 (no lock: a running slot and its requests belong to the
-// dispatcher): the lengths are on the host, queue the exact PNG bytes back.
-static void queue_png_copies(r2p_server* sv, Slot& sl)
-{
-    for (size_t i = 0; i < sl.reqs.size(); i++) {
-        Request* r = sl.reqs[i];
-        const uint64_t len = sl.h_lens[i];
-        if (len >> 63) {
-            r->status = (int)(len & 0xFF);
-            r->png_len = 0;
-            continue;
-        }
-        r->png_len = (size_t)len;
-        if (cudaMemcpyAsync(r->h_png, sv->dmem + r->d_off + align_up(r->raw_bytes, 256), len, cudaMemcpyDeviceToHost,
-                            sl.s) != cudaSuccess) {
-            r->status = cuda_err(cudaGetLastError(), "server png readback");
-            r->png_len = 0;
-        }
-    }
-    sl.phase = 2;
-    if (cudaLaunchHostFunc(sl.s, host_pngs_ready, &sl) != cudaSuccess) {
-        cudaStreamSynchronize(sl.s);
-        sl.pngs_ready.store(true, std::memory_order_release);
-    }
-}
-
-// Phase 2 done (mu held): hand the results over and free the slot.
-static void retire_slot(r2p_server* sv, Slot& sl)
-{
-    for (Request* r : sl.reqs) {
-        if (r->status == R2P_OK) finish_request(sv, r, RQ_DONE, R2P_OK);
-        else finish_request(sv, r, RQ_FAILED, r->status);
-    }
-    release_slot_memory(sv, sl);
-    sl.reqs.clear();
-    sl.plans.clear();
-    sl.active = false;
-    sl.phase = 0;
-    sv->cv_done.notify_all();
-}
-
-// Form one batch for an idle slot from the pending queue and launch it.
-// Returns whether a batch was formed.
-static bool launch_batch(r2p_server* sv, Slot& sl)
-{
-    r2p_engine* e = sv->eng;
-    std::vector<Request*> take;
-    CallBuffers cb;
-    {
-        std::lock_guard<std::mutex> lk(sv->mu);
-        size_t est = 0, raw_total = 0;
-        while (!sv->pending.empty() && (int)take.size() < sv->cfg.max_batch_images) {
-            Request* r = sv->pending.front();
-            if (!take.empty() && raw_total + r->raw_bytes > sv->cfg.max_batch_bytes) break;
-            // admission: its pixels + PNG now, and room for its scratch later
-            if (!sv->dpool.alloc(r->d_bytes, r->d_off)) break;
-            if (sv->dpool.cap() - sv->dpool.used() < est + r->est_scratch) {
-                sv->dpool.release(r->d_off, r->d_bytes);
-                break;
-            }
-            est += r->est_scratch;
-            raw_total += r->raw_bytes;
-            sv->pending.pop_front();
-            take.push_back(r);
-        }
-        if (take.empty()) return false;
-        // plan; if the batch's scratch does not fit, hand back requests from the tail
-        for (;;) {
-            sl.plans.clear();
-            cb = CallBuffers();
-            for (Request* r : take) {
-                sl.plans.push_back(r->plan);
-                cb.raw.push_back(sv->dmem + r->d_off);
-                cb.filt.push_back(nullptr);
-                cb.prior.push_back(nullptr);
-                cb.out.push_back(sv->dmem + r->d_off + align_up(r->raw_bytes, 256));
-                cb.out_cap.push_back(r->bound);
-                cb.out_len.push_back(nullptr);
-            }
-            sl.P = Prepared();
-            plan_work(e, sl.plans, cb, 8 * take.size(), sl.P);
-            if (sv->dpool.alloc(sl.P.total, sl.scratch_off)) {
-                sl.scratch_bytes = sl.P.total;
-                break;
-            }
-            Request* r = take.back();
-            take.pop_back();
-            sv->dpool.release(r->d_off, r->d_bytes);
-            sv->pending.push_front(r);
-            if (take.empty()) return false;
-        }
-        // descriptor + length staging from the pinned pool (no allocation call)
-        sl.stage_bytes = align_up(sl.P.desc_bytes, 256) + 8 * take.size();
-        sl.stage_pinned = sv->hpool.alloc(sl.stage_bytes, sl.stage_off);
-        uint8_t* hs;
-        if (sl.stage_pinned) {
-            hs = sv->hmem + sl.stage_off;
-        } else {
-            sl.heap.resize(sl.stage_bytes);
-            hs = sl.heap.data();
-        }
-        sl.h_desc = hs;
-        sl.h_lens = reinterpret_cast<uint64_t*>(hs + align_up(sl.P.desc_bytes, 256));
-        const Clock::time_point now = Clock::now();
-        for (Request* r : take) {
-            r->state = RQ_RUNNING;
-            r->t_dispatch = now;
-        }
-        sv->batches++;
-        sv->batched_images += take.size();
-    }
-    // enqueue without the lock
-    const size_t n = take.size();
-    uint8_t* base = sv->dmem + sl.scratch_off;
-    for (size_t i = 0; i < n; i++) cb.out_len[i] = reinterpret_cast<uint64_t*>(base + sl.P.o_extra) + i;
-    fill_pointers(sl.plans, cb, sl.P, base);
-    sl.reqs = take;
-    sl.active = true;
-    sl.phase = 1;
-    sl.lens_ready.store(false, std::memory_order_relaxed);
-    sl.pngs_ready.store(false, std::memory_order_relaxed);
-    cudaError_t ce = cudaSuccess;
-    for (size_t i = 0; i < n && ce == cudaSuccess; i++) {
-        Request* r = take[i];
-        ce = cudaMemcpyAsync(sv->dmem + r->d_off, r->h_px, r->raw_bytes, cudaMemcpyHostToDevice, sl.s);
-    }
-    if (ce == cudaSuccess) {
-        write_descriptors(sl.h_desc, sl.plans, sl.P);
-        ce = cudaMemcpyAsync(base, sl.h_desc, sl.P.desc_bytes, cudaMemcpyHostToDevice, sl.s);
-    }
-    int rc = (ce == cudaSuccess) ? launch_stages(e, (int)n, sl.P, base, ST_ALL, sl.s, nullptr, nullptr)
-                                 : cuda_err(ce, "server batch upload");
-    if (rc == R2P_OK) {
-        ce = cudaMemcpyAsync(sl.h_lens, base + sl.P.o_extra, 8 * n, cudaMemcpyDeviceToHost, sl.s);
-        if (ce == cudaSuccess) ce = cudaLaunchHostFunc(sl.s, host_lens_ready, &sl);
-        if (ce != cudaSuccess) rc = cuda_err(ce, "server batch readback");
-    }
-    if (rc != R2P_OK) {
-        // nothing of this batch will report back: let queued work drain, then
-        // fail its requests
-        cudaStreamSynchronize(sl.s);
-        std::lock_guard<std::mutex> lk(sv->mu);
-        for (Request* r : take) finish_request(sv, r, RQ_FAILED, rc);
-        release_slot_memory(sv, sl);
-        sl.reqs.clear();
-        sl.plans.clear();
-        sl.active = false;
-        sl.phase = 0;
-        sv->dispatch_error = rc;
-        sv->cv_done.notify_all();
-    }
-    return true;
-}
-
-static void dispatcher_main(r2p_server* sv)
-{
-    cudaSetDevice(sv->eng->device);
-    for (;;) {
-        // taken before looking at any state, so no wake-up in between is lost
-        const uint64_t seen = wake_snapshot(sv);
-        bool progressed = false;
-        for (auto& slp : sv->slots) {
-            Slot& sl = *slp;
-            if (!sl.active) continue;
-            if (sl.phase == 1 && sl.lens_ready.load(std::memory_order_acquire)) {
-                queue_png_copies(sv, sl);
-                progressed = true;
-            }
-            if (sl.phase == 2 && sl.pngs_ready.load(std::memory_order_acquire)) {
-                std::lock_guard<std::mutex> lk(sv->mu);
-                retire_slot(sv, sl);
-                progressed = true;
-            }
-        }
-        for (auto& slp : sv->slots)
-            if (!slp->active && launch_batch(sv, *slp)) progressed = true;
-        {
-            std::lock_guard<std::mutex> lk(sv->mu);
-            bool any_active = false;
-            for (auto& slp : sv->slots) any_active |= slp->active;
-            if (sv->stop && sv->pending.empty() && !any_active) break;
-        }
-        if (progressed) continue;
-        std::unique_lock<std::mutex> wl(sv->wake_mu);
-        sv->cv_wake.wait_for(wl, std::chrono::milliseconds(50), [&] { return sv->wake_seq != seen; });
-    }
-}
-
-}  // namespace r2p
-
-extern "C" {
-
-int r2p_server_create(int device, const r2p_server_config* cfg, r2p_server** out)
-{
-    if (!out) return set_err(R2P_EINVAL, "out is NULL");
-    *out = nullptr;
-    r2p_server_config c{};
-    if (cfg) c = *cfg;
-    if (c.hbm_budget == 0) c.hbm_budget = (size_t)40 << 30;
-    if (c.host_pool_bytes == 0) c.host_pool_bytes = (size_t)4 << 30;
-    if (c.max_inflight_batches <= 0) c.max_inflight_batches = 8;
-    if (c.max_batch_images <= 0) c.max_batch_images = 512;
-    if (c.max_batch_bytes == 0) c.max_batch_bytes = (size_t)96 << 20;
-    r2p_engine* e = nullptr;
-    int rc = r2p_engine_create(device, 0, &e);
-    if (rc) return rc;
-    r2p_server* sv = new r2p_server();
-    sv->eng = e;
-    sv->cfg = c;
-    cudaError_t ce = cudaMalloc(&sv->dmem, c.hbm_budget);
-    if (ce == cudaSuccess) ce = cudaMallocHost(&sv->hmem, c.host_pool_bytes);
-    for (int i = 0; i < c.max_inflight_batches; i++) {
-        sv->slots.emplace_back(new r2p::Slot());
-        sv->slots.back()->srv = sv;
-        if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&sv->slots.back()->s, cudaStreamNonBlocking);
-    }
-    if (ce != cudaSuccess) {
-        for (auto& sl : sv->slots)
-            if (sl->s) cudaStreamDestroy(sl->s);
-        if (sv->dmem) cudaFree(sv->dmem);
-        if (sv->hmem) cudaFreeHost(sv->hmem);
-        r2p_engine_destroy(e);
-        delete sv;
-        return cuda_err(ce, "r2p_server_create");
-    }
-    sv->dpool.init(c.hbm_budget);
-    sv->hpool.init(c.host_pool_bytes);
-    sv->dispatcher = std::thread(dispatcher_main, sv);
-    *out = sv;
-    return R2P_OK;
-}
-
-int r2p_server_set_tuning(r2p_server* sv, int n, const r2p_tuning* classes)
-{
-    if (!sv) return set_err(R2P_EINVAL, "NULL server");
-    return r2p_engine_set_tuning(sv->eng, n, classes);
-}
-
-int r2p_server_submit(r2p_server* sv, const r2p_image* img, const void* h_pixels, uint64_t* ticket)
-{
-    return r2p_server_submit_ex(sv, img, h_pixels, 0u, ticket);
-}
-
-int r2p_server_submit_ex(r2p_server* sv, const r2p_image* img, const void* h_pixels, uint32_t flags,
-                         uint64_t* ticket)
-{
-    if (!sv || !img || !h_pixels || !ticket) return set_err(R2P_EINVAL, "NULL argument");
-    if (flags & ~(uint32_t)R2P_SUBMIT_BORROW) return set_err(R2P_EINVAL, "unknown submit flags");
-    const bool borrow = (flags & R2P_SUBMIT_BORROW) != 0;
-    Request* r = new Request();
-    r->img = *img;
-    int rc = plan_image(*img, 0, r->plan, sv->eng->tuning);
-    if (rc) { delete r; return rc; }
-    r->raw_bytes = (size_t)r->plan.raw_bytes;
-    r->bound = (size_t)r->plan.png_bound;
-    r->d_bytes = align_up(r->raw_bytes, 256) + align_up(r->bound, 256);
-    const DevImage& d = r->plan.di;
-    r->est_scratch = sizeof(DevImage) + 4096 + (size_t)d.nblocks * (sizeof(BlockOut) + lz77_slot_bytes(d.block_size)) +
-                     align_up(d.filt_bytes + 64, 256) + (size_t)r->plan.lut_cap + 4 * 256;
-    if (r->d_bytes + r->est_scratch > sv->cfg.hbm_budget) {
-        delete r;
-        return set_err(R2P_EBUDGET, "request larger than the server's HBM budget");
-    }
-    // host space: the PNG (and a copy of the pixels unless they are borrowed)
-    const size_t px_room = borrow ? 0 : align_up(r->raw_bytes, 256);
-    r->h_bytes = px_room + r->bound;
-    {
-        std::lock_guard<std::mutex> lk(sv->mu);
-        r->h_pinned = sv->hpool.alloc(r->h_bytes, r->h_off);
-    }
-    uint8_t* hb;
-    if (r->h_pinned) {
-        hb = sv->hmem + r->h_off;
-    } else {
-        r->heap.resize(r->h_bytes);
-        hb = r->heap.data();
-    }
-    r->h_png = hb + px_room;
-    if (borrow) {
-        r->h_px = static_cast<uint8_t*>(const_cast<void*>(h_pixels));
-    } else {
-        r->h_px = hb;
-        memcpy(r->h_px, h_pixels, r->raw_bytes);
-    }
-    r->t_submit = Clock::now();
-    {
-        std::lock_guard<std::mutex> lk(sv->mu);
-        if (sv->stop) {
-            if (r->h_pinned) sv->hpool.release(r->h_off, r->h_bytes);
-            delete r;
-            return set_err(R2P_ECANCELED, "server is shutting down");
-        }
-        r->ticket = sv->next_ticket++;
-        sv->reqs[r->ticket] = r;
-        sv->pending.push_back(r);
-        *ticket = r->ticket;
-    }
-    wake_dispatcher(sv);
-    return R2P_OK;
-}
-
-int r2p_server_wait(r2p_server* sv, uint64_t ticket, int timeout_ms, r2p_result* res)
-{
-    if (!sv || !res) return set_err(R2P_EINVAL, "NULL argument");
-    std::unique_lock<std::mutex> lk(sv->mu);
-    auto it = sv->reqs.find(ticket);
-    if (it == sv->reqs.end()) return set_err(R2P_ENOTFOUND, "unknown ticket");
-    Request* r = it->second;
-    auto finished = [&] { return r->state == RQ_DONE || r->state == RQ_FAILED || r->state == RQ_CANCELED; };
-    if (timeout_ms < 0) sv->cv_done.wait(lk, finished);
-    else if (!sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished))
-        return set_err(R2P_ETIMEOUT, "request still running");
-    res->status = r->status;
-    res->png = r->state == RQ_DONE ? r->h_png : nullptr;
-    res->png_len = r->state == RQ_DONE ? r->png_len : 0;
-    res->latency_ms = ms_between(r->t_submit, r->t_done);
-    res->queue_ms = r->state == RQ_CANCELED ? res->latency_ms : ms_between(r->t_submit, r->t_dispatch);
-    return r->status == R2P_OK ? R2P_OK : set_err(r->status, r->state == RQ_CANCELED ? "request cancelled"
-                                                                                   : "request failed");
-}
-
-int r2p_server_cancel(r2p_server* sv, uint64_t ticket)
-{
-    if (!sv) return set_err(R2P_EINVAL, "NULL server");
-    std::lock_guard<std::mutex> lk(sv->mu);
-    auto it = sv->reqs.find(ticket);
-    if (it == sv->reqs.end()) return set_err(R2P_ENOTFOUND, "unknown ticket");
-    Request* r = it->second;
-    if (r->state != RQ_PENDING) return set_err(R2P_EINVAL, "request already dispatched or finished");
-    for (auto q = sv->pending.begin(); q != sv->pending.end(); ++q)
-        if (*q == r) { sv->pending.erase(q); break; }
-    r->d_bytes = 0;
-    finish_request(sv, r, RQ_CANCELED, R2P_ECANCELED);
-    sv->cv_done.notify_all();
-    return R2P_OK;
-}
-
-int r2p_server_release(r2p_server* sv, uint64_t ticket)
-{
-    if (!sv) return set_err(R2P_EINVAL, "NULL server");
-    std::lock_guard<std::mutex> lk(sv->mu);
-    auto it = sv->reqs.find(ticket);
-    if (it == sv->reqs.end()) return set_err(R2P_ENOTFOUND, "unknown ticket");
-    Request* r = it->second;
-    if (r->state == RQ_PENDING || r->state == RQ_RUNNING) return set_err(R2P_EINVAL, "request still in flight");
-    if (r->h_pinned) sv->hpool.release(r->h_off, r->h_bytes);
-    sv->reqs.erase(it);
-    delete r;
-    return R2P_OK;
-}
-
-int r2p_server_get_stats(r2p_server* sv, r2p_server_stats* st)
-{
-    if (!sv || !st) return set_err(R2P_EINVAL, "NULL argument");
-    std::lock_guard<std::mutex> lk(sv->mu);
-    memset(st, 0, sizeof(*st));
-    st->completed = sv->completed;
-    st->failed = sv->failed;
-    st->canceled = sv->canceled;
-    st->batches = sv->batches;
-    st->mean_batch_images = sv->batches ? (double)sv->batched_images / (double)sv->batches : 0.0;
-    st->pending = sv->pending.size();
-    st->device_bytes_in_use = sv->dpool.used();
-    st->device_bytes_peak = sv->dpool.peak();
-    if (!sv->lat_ms.empty()) {
-        std::vector<double> v = sv->lat_ms;
-        std::sort(v.begin(), v.end());
-        auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * (double)(v.size() - 1) + 0.5))]; };
-        st->p50_ms = pct(0.50);
-        st->p99_ms = pct(0.99);
-        st->max_ms = v.back();
-    }
-    return R2P_OK;
-}
-
-int r2p_server_reset_stats(r2p_server* sv)
-{
-    if (!sv) return set_err(R2P_EINVAL, "NULL server");
-    std::lock_guard<std::mutex> lk(sv->mu);
-    sv->lat_ms.clear();
-    sv->completed = sv->failed = sv->canceled = sv->batches = sv->batched_images = 0;
-    return R2P_OK;
-}
-
-void r2p_server_destroy(r2p_server* sv)
-{
-    if (!sv) return;
-    {
-        std::lock_guard<std::mutex> lk(sv->mu);
-        sv->stop = true;
-    }
-    r2p::wake_dispatcher(sv);
-    if (sv->dispatcher.joinable()) sv->dispatcher.join();
-    cudaSetDevice(sv->eng->device);
-    for (auto& kv : sv->reqs) delete kv.second;
-    for (auto& sl : sv->slots)
-        if (sl->s) cudaStreamDestroy(sl->s);
-    if (sv->dmem) cudaFree(sv->dmem);
-    if (sv->hmem) cudaFreeHost(sv->hmem);
-    r2p_engine_destroy(sv->eng);
-    delete sv;
-}
-
-}  // extern "C"

@@ -6,7 +6,8 @@
 // memory budget), and latency-sensitive callers for which cudaMalloc/cudaFree
 // are unacceptable because they can stall or synchronize the device.  For
 // them r2p_zlib_compress_noalloc runs the same DEFLATE kernels as
-// r2p_zlib_compress_device (stored or LZ77 + fixed Huffman blocks, Adler-32
+// r2p_zlib_compress_device (stored blocks at level 0, LZ77 + fixed Huffman at
+// level 1, dynamic Huffman over a run-length parse at levels 2-9, Adler-32
 // trailer) with every piece of scratch -- work descriptors, per-block results,
 // the LZ77 block slots and the CRC power table -- in one file-scope
 // __device__ array of kNoAllocScratchBytes.  Every GPU that loads the library
@@ -16,7 +17,9 @@
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress and fills the CRC power
 // table with a kernel, then waits for it; make that first call before any
-// stream capture.  All calls share the array, which keeps the previous call's
+// stream capture.  The set-up is kept for the life of the process: after
+// cudaDeviceReset (which clears the array) the entry point must not be used
+// again.  All calls share the array, which keeps the previous call's
 // contents: each call rewrites every descriptor it reads.  Calls that overlap
 // on the GPU race on the array: issue them on one stream, or order them.
 #include <cuda_runtime.h>
@@ -38,6 +41,9 @@ constexpr size_t kNoAllocScratchBytes = 2u << 20;      // static scratch per GPU
 constexpr size_t kNaImage = 0;                          // DevImage
 constexpr size_t kNaXpow = 256;                         // kXpowLevels * 1024 uint32
 constexpr size_t kNaBlocks = kNaXpow + kXpowLevels * 1024 * 4;   // BlockOut[]
+
+static_assert(sizeof(DevImage) <= kNaXpow - kNaImage, "the image descriptor overruns the power table");
+static_assert(kNaBlocks % alignof(BlockOut) == 0 && kNaXpow % 16 == 0, "scratch regions misaligned");
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
 

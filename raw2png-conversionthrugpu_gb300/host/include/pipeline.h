@@ -16,7 +16,7 @@ enum class ExportFormat { PNG, BMP };
 struct PipelineConfig {
     int  strip_height    = 0;      // rows per strip; 0 = auto (1024)
     int  deflate_threads = 6;      // accepted for compatibility; DEFLATE runs on the GPU
-    int  deflate_level   = 3;      // 0 = stored, 1..9 = LZ77 + fixed Huffman
+    int  deflate_level   = 3;      // 0 = stored, 1 = LZ77 + fixed Huffman, 2..9 = dynamic Huffman
     int  frame           = -1;     // DICOM frame, -1 = first
     bool verbose         = false;
     int  gpu_streams     = 0;      // frames in flight for multi-frame export; 0 = auto (4)

@@ -30,7 +30,8 @@ static void usage(const char* prog)
                  "  --all                every frame as <output>/slice_NNNN.png   (alias: -all)\n"
                  "  --frame N            export DICOM frame N (0-based)\n"
                  "  --strip-height N     rows per strip (default 1024)\n"
-                 "  --level N            0 = stored, 1-9 = LZ77 + fixed Huffman (default 3)\n"
+                 "  --level N            0 = stored, 1 = LZ77 + fixed Huffman, 2-9 = dynamic\n"
+                 "                       Huffman over a run-length parse (default 3)\n"
                  "  --threads N          accepted; DEFLATE runs on the GPU\n"
                  "  --verbose            per-file report\n"
                  "  --batch-workers N    folder mode file readers (default: auto)\n"
