@@ -17,8 +17,10 @@
 // of the block sequentially (32 warps per SM: the parse is latency-bound, so
 // the warps hide each other's dependency chains) -- a
 // greedy LZ77 with two candidates per position: distance 1 (a run) and the
-// head of a 4-byte hash table shared by the 32 lanes of a warp (seeded from
-// the ~2 KB before the warp's range).  The PNG filter has already taken the
+// head of a 3-byte hash table shared by the 32 lanes of a warp (seeded from
+// the ~2 KB before the warp's range); a match is taken when it is at least 4
+// bytes long, or 3 within 4096 bytes back (where its code, at most 22 bits,
+// is shorter than three literals).  The PNG filter has already taken the
 // scanline above out of the bytes, so a third candidate one scanline up found
 // almost nothing the hash did not (990 of 12.55 M bytes on a 3072x3072 16-bit
 // image) and cost a tenth of the launch; it is not searched.
@@ -49,6 +51,7 @@ constexpr int kLzThreads = kLzWarps * 32;
 constexpr int kPrefill = 4096;        // history bytes hashed before a warp's range
 constexpr int kMaxDist = 32768;
 constexpr int kMaxMatch = 258;
+constexpr int kFar3 = 4096;           // farthest 3-byte match taken: nearer ones are shorter than 3 literals
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 
 // Bytes each thread parses in a block of n bytes: a multiple of 4 whose word
@@ -91,8 +94,8 @@ __device__ __forceinline__ uint32_t ld32u(const uint8_t* base, int p)
     return fshr(w[q], w[q + 1], (uint32_t)(p & 3) << 3);
 }
 
-// Multiplicative hash of 4 bytes to hb bits.
-__device__ __forceinline__ uint32_t hash4(uint32_t v, int hb) { return (v * 2654435761u) >> (32 - hb); }
+// Multiplicative hash of the low 3 bytes (the shortest match) to hb bits.
+__device__ __forceinline__ uint32_t hash3(uint32_t v, int hb) { return ((v & 0xFFFFFFu) * 2654435761u) >> (32 - hb); }
 
 // An image's hash table bits: 9 or 10 (32 warps of 2^10 u16 entries fit beside
 // a 64 KB block; 11 bits would not).
@@ -182,16 +185,26 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t
     while (p + 4 <= e) {
         int L = 0, D = 0;
         {
-            const uint32_t h = hash4(w, hb);
+            const uint32_t h = hash3(w, hb);
             const int t = tab[h];
             tab[h] = (uint16_t)(p + 1);
-            if (w == prev * 0x01010101u) {
-                D = 1;
+            const uint32_t rx = w ^ (prev * 0x01010101u);
+            if (rx == 0u) {
+                D = 1;                              // a run of 4 or more
             } else {
                 const int dist = p - (t - 1);       // <= 0: a later position of another lane, or empty
-                if (dist > 0 && ld32u(in, t - 1) == w) D = dist;
+                const uint32_t hx = dist > 0 ? (ld32u(in, t - 1) ^ w) : 1u;
+                if (hx == 0u) {
+                    D = dist;                       // 4 or more equal bytes
+                } else if ((rx & 0xFFFFFFu) == 0u) {
+                    L = 3;                          // a run of exactly 3
+                    D = 1;
+                } else if ((hx & 0xFFFFFFu) == 0u && dist <= kFar3) {
+                    L = 3;                          // 3 equal bytes, near enough to pay
+                    D = dist;
+                }
             }
-            if (D) {
+            if (D && !L) {
                 // extend by words, then bytes, up to the sub-range end
                 const int maxl = min(kMaxMatch, e - p);
                 if (D == 1) {
@@ -219,7 +232,7 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t
         }
         uint32_t v;
         int nb;
-        if (L >= 4) {
+        if (L >= 3) {
             match_code(L, D, lt, dt, v, nb);
             p += L;
             w = ld32u(in, p);
@@ -333,7 +346,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
                 const uint32_t lo = w32[q >> 2], hi = w32[(q >> 2) + 1];
 #pragma unroll
                 for (int j = 0; j < 4; j++)
-                    if (q + j + 4 <= n) mytab[hash4(fshr(lo, hi, 8u * j), hb)] = (uint16_t)(q + j + 1);
+                    if (q + j + 4 <= n) mytab[hash3(fshr(lo, hi, 8u * j), hb)] = (uint16_t)(q + j + 1);
             }
             __syncwarp();
         }
