@@ -242,7 +242,7 @@ def measure_c3(r2p, W, eng, stream, n=1000, reps=3):
     filt_total = sum(im.filtered_bytes for im in imgs)
     stream_total = png_bytes - 63 * n
     alg = {"window_filter": raw_bytes + filt_total, "lz77_blocks": filt_total + stream_total,
-           "stored_blocks": 2 * filt_total, "copy_blocks": 2 * stream_total, "finalize": 0, "prepare_window": 0}
+           "stored_blocks": 2 * filt_total, "finish": 2 * stream_total, "prepare_window": 0, "unused": 0}
     dname, (dms, _) = max(st.items(), key=lambda kv: kv[1][0])
     peak, peak_kind = peaks()
     kname = r2p.filter_kernel(imgs[0]) if dname == "window_filter" else r2p.KERNELS[r2p.STAGES.index(dname)]
@@ -754,8 +754,8 @@ def run_ours(args):
     alg = {"window_filter": img.raw_bytes + img.filtered_bytes,
            "lz77_blocks": img.filtered_bytes + stream_bytes,
            "stored_blocks": img.filtered_bytes + stream_bytes,
-           "copy_blocks": 2 * stream_bytes,
-           "finalize": 0, "prepare_window": 0}
+           "finish": 2 * stream_bytes,
+           "prepare_window": 0, "unused": 0}
     achieved = alg[dname] / (per_launch_ms / 1e3) / 1e9
     kname = r2p.filter_kernel(img) if dname == "window_filter" else r2p.KERNELS[r2p.STAGES.index(dname)]
     stage_ms = {k: round(v[0] / max(v[1], 1), 5) for k, v in stages.items() if v[1]}

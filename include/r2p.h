@@ -352,8 +352,8 @@ int  r2p_stream_wait_event(void* stream, void* ev);   /* later work on stream wa
 #define R2P_STAGE_FILTER   1   /* k_window_filter / k_window_filter_reg: window + adaptive filter */
 #define R2P_STAGE_STORED   2   /* k_stored_blocks: level-0 DEFLATE */
 #define R2P_STAGE_LZ77     3   /* k_lz77_blocks (level 1) and k_rle_dyn_blocks (2..9) */
-#define R2P_STAGE_FINALIZE 4   /* k_finalize: checksums + PNG chunks */
-#define R2P_STAGE_COPY     5   /* k_copy_blocks: block gather */
+#define R2P_STAGE_FINALIZE 4   /* k_finish: block gather, checksum combine, PNG chunks */
+#define R2P_STAGE_COPY     5   /* always 0: the block gather runs inside k_finish */
 #define R2P_STAGE_COUNT    6
 int r2p_engine_set_timing(r2p_engine* eng, int enable);
 int r2p_engine_stage_times(r2p_engine* eng, double* ms, uint64_t* launches);

@@ -207,8 +207,8 @@ SIGNATURES = {
     "r2p_engine_stage_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _u64p]),
 }
 
-STAGES = ["prepare_window", "window_filter", "stored_blocks", "lz77_blocks", "finalize", "copy_blocks"]
-KERNELS = ["k_prepare_window", "k_window_filter", "k_stored_blocks", "k_lz77_blocks", "k_finalize", "k_copy_blocks"]
+STAGES = ["prepare_window", "window_filter", "stored_blocks", "lz77_blocks", "finish", "unused"]
+KERNELS = ["k_prepare_window", "k_window_filter", "k_stored_blocks", "k_lz77_blocks", "k_finish", None]
 
 
 def filter_kernel(img):

@@ -1,4 +1,4 @@
-// k_deflate.cu -- stored DEFLATE blocks, per-image PNG finalize, block copy,
+// k_deflate.cu -- stored DEFLATE blocks, the finish pass (block gather, checksum combine, PNG chunks),
 // and standalone Adler-32 / CRC-32 over device data.
 //
 // Reference semantics:
@@ -11,9 +11,12 @@
 //                           colour type from channels (src/pipeline.cpp:80-88)
 //
 // Every block kernel leaves per-block partials (output length, CRC of its
-// output bytes, Adler sums of its input bytes); k_finalize joins them with the
-// combine identities, so no kernel waits on another block.
+// output bytes, Adler sums of its input bytes); k_finish joins them with the
+// combine identities and gathers the blocks, so no kernel waits on another
+// block.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "k_deflate.cuh"
 #include "r2p_kernels.h"
@@ -84,10 +87,12 @@ __device__ __forceinline__ void put_be32(uint8_t* p, uint32_t v)
     p[0] = (uint8_t)(v >> 24); p[1] = (uint8_t)(v >> 16); p[2] = (uint8_t)(v >> 8); p[3] = (uint8_t)v;
 }
 
-constexpr int kFinThreads = 1024;   // one block per thread up to 1024 blocks: the GF(2) shifts run side by side
+constexpr int kFinThreads = 1024;   // standalone checksum combine: one partial per thread
+constexpr int kFinishThreads = 256;
 
-// Exclusive scan of a per-thread u64 value across the CTA; returns the
-// exclusive prefix and writes the CTA total to *total.
+// Exclusive scan of a per-thread u64 value across an NT-thread CTA; returns
+// the exclusive prefix and writes the CTA total to *total.
+template <int NT>
 __device__ uint64_t cta_exscan64(uint64_t v, uint64_t* sw, uint64_t* total)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -100,7 +105,8 @@ __device__ uint64_t cta_exscan64(uint64_t v, uint64_t* sw, uint64_t* total)
     if (lane == 31) sw[warp] = x;
     __syncthreads();
     uint64_t base = 0, tot = 0;
-    for (int i = 0; i < kFinThreads / 32; i++) {
+#pragma unroll
+    for (int i = 0; i < NT / 32; i++) {
         if (i < warp) base += sw[i];
         tot += sw[i];
     }
@@ -109,111 +115,138 @@ __device__ uint64_t cta_exscan64(uint64_t v, uint64_t* sw, uint64_t* total)
     return base + x - v;
 }
 
-// Per image: stream offsets of its blocks, Adler-32 of the filtered bytes,
-// CRC-32 of the IDAT chunk, and the PNG chunks around the DEFLATE stream.
-// Output layout: sig | IHDR | IDAT len,type | zlib hdr | stream | adler | crc | IEND.
-__global__ void __launch_bounds__(kFinThreads)
-k_finalize(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, const uint32_t* __restrict__ xpow)
+// Bytes an image's output needs for a DEFLATE stream of Ls bytes: the PNG
+// chunks around it, the zlib header and Adler trailer, or for raw DEFLATE the
+// stream and the input's Adler-32 after it.
+__device__ __forceinline__ uint64_t output_need(const DevImage& d, uint64_t Ls)
 {
-    DevImage& d = imgs[blockIdx.x];
-    BlockOut* B = blocks + d.blk0;
+    return d.out_kind == 0 ? (uint64_t)kPngPrefix + Ls + kPngSuffix : d.out_kind == 2 ? Ls + 4 : 2 + Ls + 4;
+}
+
+// One image's stream offsets, Adler-32 of the filtered bytes, CRC-32 of the
+// IDAT chunk, and the PNG chunks around the DEFLATE stream of Ls bytes.
+// Output layout: sig | IHDR | IDAT len,type | zlib hdr | stream | adler | crc | IEND.
+// Whole CTA; tab holds the slicing tables.
+template <int NT>
+__device__ void finish_image(DevImage& d, BlockOut* B, uint64_t Ls, const uint32_t* __restrict__ xpow,
+                             const uint32_t (*tab)[256], uint64_t* sw, uint64_t* red64, uint32_t* red32)
+{
     const int nb = d.nblocks;
-    __shared__ uint64_t sw[kFinThreads / 32];
-    __shared__ uint64_t red64[kFinThreads / 32];
-    __shared__ uint32_t red32[kFinThreads / 32];
-    __shared__ uint32_t tab[4][256];
-    build_crc_tables(tab);
-    // 1. stream offsets
-    uint64_t carry = 0;
-    for (int base = 0; base < nb; base += kFinThreads) {
+    const uint64_t F = d.filt_bytes;
+    uint64_t s1 = 0, s2 = 0, carry = 0;
+    uint32_t cx = 0;
+    for (int base = 0; base < nb; base += NT) {
         const int i = base + threadIdx.x;
         const uint64_t len = (i < nb) ? B[i].out_len : 0;
         uint64_t tot;
-        const uint64_t ex = cta_exscan64(len, sw, &tot);
-        if (i < nb) B[i].out_off = carry + ex;
+        const uint64_t off = carry + cta_exscan64<NT>(len, sw, &tot);
         carry += tot;
+        if (i < nb) {
+            BlockOut& bo = B[i];
+            bo.out_off = off;
+            const uint64_t after_in = F - (uint64_t)bo.in_off - bo.in_len;
+            s1 += bo.s1;
+            s2 = (s2 + bo.s2 % kAdlerMod + (after_in % kAdlerMod) * (bo.s1 % kAdlerMod)) % kAdlerMod;
+            const uint64_t after_out = Ls - off - len + 4;   // + Adler trailer
+            cx ^= gf2_mulmod_t(bo.crc, xpow8n_t(after_out, xpow, tab), tab);
+        }
     }
-    const uint64_t Ls = carry;                   // DEFLATE stream bytes
-    __syncthreads();
-    // 2. Adler-32 sums and CRC pieces
-    uint64_t s1 = 0, s2 = 0;
-    uint32_t cx = 0;
-    const uint64_t F = d.filt_bytes;
-    for (int i = threadIdx.x; i < nb; i += kFinThreads) {
-        const BlockOut& bo = B[i];
-        const uint64_t after_in = F - (uint64_t)bo.in_off - bo.in_len;
-        s1 += bo.s1;
-        s2 = (s2 + bo.s2 % kAdlerMod + (after_in % kAdlerMod) * (bo.s1 % kAdlerMod)) % kAdlerMod;
-        const uint64_t after_out = Ls - bo.out_off - bo.out_len + 4;   // + Adler trailer
-        cx ^= gf2_mulmod_t(bo.crc, xpow8n_t(after_out, xpow, tab), tab);
+    s1 = cta_sum64<NT>(s1, red64);
+    s2 = cta_sum64<NT>(s2, red64);
+    cx = cta_xor<NT>(cx, red32);
+    if (threadIdx.x != 0) return;
+    const bool png = (d.out_kind == 0), raw = (d.out_kind == 2);
+    const uint64_t total = raw ? Ls : output_need(d, Ls);   // raw: the Adler word is not counted
+    if (d.status == 0 && output_need(d, Ls) > d.png_cap) d.status = R2P_ENOSPC;
+    if (d.status) {                    // error word: top bit set, status in the low bits
+        *d.png_len = (1ull << 63) | (uint64_t)d.status;
+        return;
     }
-    s1 = cta_sum64<kFinThreads>(s1, red64);
-    s2 = cta_sum64<kFinThreads>(s2, red64);
-    cx = cta_xor<kFinThreads>(cx, red32);
-    if (threadIdx.x == 0) {
-        const bool png = (d.out_kind == 0), raw = (d.out_kind == 2);
-        // raw DEFLATE: the input's Adler-32 follows the stream (4 bytes, big-endian, not counted)
-        const uint64_t total = png ? (uint64_t)kPngPrefix + Ls + kPngSuffix : raw ? Ls : 2 + Ls + 4;
-        if (d.status == 0 && total + (raw ? 4 : 0) > d.png_cap) d.status = R2P_ENOSPC;
-        if (d.status) {                    // error word: top bit set, status in the low bits
-            *d.png_len = (1ull << 63) | (uint64_t)d.status;
-            return;
-        }
-        const uint32_t adler = adler_from_sums(s1, s2 % kAdlerMod, F);
-        const uint32_t (*tab0)[256] = tab;
-        uint8_t* p = d.png;
-        uint8_t head[6] = {'I', 'D', 'A', 'T', 0x78, zlib_flg(d.level)};
-        uint8_t trl[4];
-        put_be32(trl, adler);
-        uint8_t* q = p + d.prefix + Ls;
-        for (int i = 0; i < 4; i++) q[i] = trl[i];
-        if (raw) {
-            *d.png_len = total;
-            return;
-        }
-        if (!png) {
-            p[0] = head[4];
-            p[1] = head[5];
-            *d.png_len = total;
-            return;
-        }
-        const uint8_t sig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
-        for (int i = 0; i < 8; i++) p[i] = sig[i];
-        uint8_t ihdr[17] = {'I', 'H', 'D', 'R'};
-        put_be32(ihdr + 4, d.width);
-        put_be32(ihdr + 8, d.height);
-        ihdr[12] = (uint8_t)(8 * d.ob);
-        ihdr[13] = (uint8_t)(d.channels == 1 ? 0 : d.channels == 3 ? 2 : d.channels == 4 ? 6 : 2);
-        ihdr[14] = 0; ihdr[15] = 0; ihdr[16] = 0;
-        put_be32(p + 8, 13);
-        for (int i = 0; i < 17; i++) p[12 + i] = ihdr[i];
-        put_be32(p + 29, crc_small(ihdr, 17, tab0));
-        put_be32(p + 33, (uint32_t)(Ls + 6));
-        for (int i = 0; i < 6; i++) p[37 + i] = head[i];
-        const uint32_t ch = crc_small(head, 6, tab0);
-        const uint32_t ct = crc_small(trl, 4, tab0);
-        const uint32_t crc = gf2_mulmod_t(ch, xpow8n_t(Ls + 4, xpow, tab), tab) ^ cx ^ ct;
-        put_be32(q + 4, crc);
-        const uint8_t iend[12] = {0, 0, 0, 0, 'I', 'E', 'N', 'D', 0xAE, 0x42, 0x60, 0x82};
-        for (int i = 0; i < 12; i++) q[8 + i] = iend[i];
+    const uint32_t adler = adler_from_sums(s1, s2 % kAdlerMod, F);
+    uint8_t* p = d.png;
+    uint8_t head[6] = {'I', 'D', 'A', 'T', 0x78, zlib_flg(d.level)};
+    uint8_t trl[4];
+    put_be32(trl, adler);
+    uint8_t* q = p + d.prefix + Ls;
+    for (int i = 0; i < 4; i++) q[i] = trl[i];
+    if (raw) {
         *d.png_len = total;
+        return;
     }
+    if (!png) {
+        p[0] = head[4];
+        p[1] = head[5];
+        *d.png_len = total;
+        return;
+    }
+    const uint8_t sig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
+    for (int i = 0; i < 8; i++) p[i] = sig[i];
+    uint8_t ihdr[17] = {'I', 'H', 'D', 'R'};
+    put_be32(ihdr + 4, d.width);
+    put_be32(ihdr + 8, d.height);
+    ihdr[12] = (uint8_t)(8 * d.ob);
+    ihdr[13] = (uint8_t)(d.channels == 1 ? 0 : d.channels == 3 ? 2 : d.channels == 4 ? 6 : 2);
+    ihdr[14] = 0; ihdr[15] = 0; ihdr[16] = 0;
+    put_be32(p + 8, 13);
+    for (int i = 0; i < 17; i++) p[12 + i] = ihdr[i];
+    put_be32(p + 29, crc_small(ihdr, 17, tab));
+    put_be32(p + 33, (uint32_t)(Ls + 6));
+    for (int i = 0; i < 6; i++) p[37 + i] = head[i];
+    const uint32_t ch = crc_small(head, 6, tab);
+    const uint32_t ct = crc_small(trl, 4, tab);
+    const uint32_t crc = gf2_mulmod_t(ch, xpow8n_t(Ls + 4, xpow, tab), tab) ^ cx ^ ct;
+    put_be32(q + 4, crc);
+    const uint8_t iend[12] = {0, 0, 0, 0, 'I', 'E', 'N', 'D', 0xAE, 0x42, 0x60, 0x82};
+    for (int i = 0; i < 12; i++) q[8 + i] = iend[i];
+    *d.png_len = total;
 }
 
-constexpr int kCopyThreads = 256;
-
-// LZ77 path: move each block's compressed bytes from its scratch slot to its
-// stream offset in the PNG.
-__global__ void __launch_bounds__(kCopyThreads)
-k_copy_blocks(const DevImage* __restrict__ imgs, const BlockOut* __restrict__ blocks, int nblocks,
-              const uint8_t* __restrict__ scratch, uint64_t slot_bytes)
+// After the block kernels, one launch finishes every image.  A work unit is
+// one of `parts` slices of one block.  Its CTA sums the output lengths of
+// the image's blocks (the block's stream offset and the stream length) and
+// moves its slice of the block's compressed bytes from the scratch slot to
+// the PNG; the unit of an image's first block, slice 0, also writes that
+// image's checksums and chunks.  No unit waits on another: every unit
+// derives the same offsets and the same fits-the-output decision from the
+// per-block lengths.  Slices split at 16-byte steps of the slot, so each
+// slice's source stays aligned; stored (level-0) blocks are already in place.
+__global__ void __launch_bounds__(kFinishThreads)
+k_finish(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks, int parts,
+         const uint8_t* __restrict__ scratch, uint64_t slot_bytes, const uint32_t* __restrict__ xpow)
 {
-    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        const BlockOut& bo = blocks[b];
-        const DevImage& d = imgs[bo.img];
-        if (d.status || d.level == 0) continue;   // stored blocks are already in place
-        cta_copy_to_global<kCopyThreads>(d.png + d.prefix + bo.out_off, scratch + (size_t)b * slot_bytes,
-                                         (int)bo.out_len);
+    constexpr int NT = kFinishThreads;
+    __shared__ uint64_t sw[NT / 32];
+    __shared__ uint64_t red64[NT / 32];
+    __shared__ uint32_t red32[NT / 32];
+    __shared__ uint32_t tab[4][256];
+    bool have_tab = false;
+    const int units = nblocks * parts;
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+        const int b = u / parts, part = u - b * parts;
+        const int n = (int)blocks[b].out_len;
+        DevImage& d = imgs[blocks[b].img];
+        BlockOut* B = blocks + d.blk0;
+        const int nb = d.nblocks, local = b - d.blk0;
+        const int st0 = d.status;
+        uint64_t before = 0, all = 0;
+        for (int i = threadIdx.x; i < nb; i += NT) {
+            const uint64_t len = B[i].out_len;
+            all += len;
+            if (i < local) before += len;
+        }
+        before = cta_sum64<NT>(before, red64);
+        all = cta_sum64<NT>(all, red64);
+        if (local == 0 && part == 0) {
+            if (!have_tab) {
+                build_crc_tables(tab);
+                have_tab = true;
+            }
+            finish_image<NT>(d, B, all, xpow, tab, sw, red64, red32);
+        }
+        if (st0 != 0 || d.level == 0 || output_need(d, all) > d.png_cap) continue;
+        const int c0 = (int)(((int64_t)n * part / parts) & ~15ll);
+        const int c1 = (part + 1 == parts) ? n : (int)(((int64_t)n * (part + 1) / parts) & ~15ll);
+        cta_copy_to_global<NT>(d.png + d.prefix + before + c0, scratch + (size_t)b * slot_bytes + c0, c1 - c0);
     }
 }
 
@@ -306,19 +339,20 @@ cudaError_t launch_stored(const DevImage* imgs, BlockOut* blocks, int nblocks, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(DevImage* imgs, int nimg, BlockOut* blocks, const uint32_t* xpow, cudaStream_t s)
+cudaError_t launch_finish(DevImage* imgs, BlockOut* blocks, int nblocks, int parts, const uint8_t* scratch,
+                          uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s)
 {
-    k_finalize<<<nimg, kFinThreads, 0, s>>>(imgs, blocks, xpow);
+    if (parts < 1 || parts > 64 || nblocks < 1 || grid < 1) return cudaErrorInvalidValue;
+    k_finish<<<grid, kFinishThreads, 0, s>>>(imgs, blocks, nblocks, parts, scratch, slot_bytes, xpow);
     note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_copy_blocks(const DevImage* imgs, const BlockOut* blocks, int nblocks,
-                               const uint8_t* scratch, uint64_t slot_bytes, int grid, cudaStream_t s)
+int finish_parts(int nblocks, int nsm)
 {
-    k_copy_blocks<<<grid, kCopyThreads, 0, s>>>(imgs, blocks, nblocks, scratch, slot_bytes);
-    note_launch();
-    return cudaGetLastError();
+    // about eight units per SM when blocks are few; one unit per block otherwise
+    const int want = (8 * nsm + nblocks - 1) / std::max(nblocks, 1);
+    return std::min(8, std::max(1, want));
 }
 
 size_t checksum_scratch_bytes(uint64_t len)

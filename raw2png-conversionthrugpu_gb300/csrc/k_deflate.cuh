@@ -1,5 +1,5 @@
 // k_deflate.cuh -- device routines shared by the DEFLATE-side kernels
-// (stored blocks, LZ77 blocks, PNG finalize, copies, checksums).
+// (stored blocks, LZ77 blocks, the finish pass, copies, checksums).
 #pragma once
 #include <cuda_runtime.h>
 

@@ -89,7 +89,7 @@ struct BlockOut {
     uint32_t crc;          // crc32 of the compressed bytes
     uint32_t s1;           // sum of input bytes
     uint64_t s2;           // sum of (in_len - i) * d_i over the block
-    uint64_t out_off;      // offset of the block in the DEFLATE stream (set by finalize)
+    uint64_t out_off;      // offset of the block in the DEFLATE stream (set by k_finish)
 };
 
 // PNG prefix: signature (8) + IHDR chunk (25) + IDAT length/type (8) + zlib header (2)

@@ -8,9 +8,10 @@
 // bands for the filter kernel, DEFLATE blocks), uploads it in one copy, and
 // launches one kernel per stage over the whole work list:
 //   [k_prepare_window ->] k_window_filter_reg | k_window_filter
-//   -> k_stored_blocks | k_lz77_blocks | k_rle_dyn_blocks -> k_finalize
-//   -> (k_copy_blocks)
-// (k_prepare_window builds window tables in HBM for the shared-memory filter
+//   -> k_stored_blocks | k_lz77_blocks | k_rle_dyn_blocks -> k_finish
+// (k_finish gathers the compressed blocks into the output, joins the
+// per-block checksums and writes the PNG chunks;
+// k_prepare_window builds window tables in HBM for the shared-memory filter
 // kernel and the BMP export; the register-resident kernel builds its own.)
 // Calls are ordered through the engine: each call waits (on the device, not
 // the host) for the previous call's last kernel before reusing the arena.
@@ -469,11 +470,14 @@ int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stage
         R2P_CU(launch_dyn(dimg, dblocks, (int)P.nblk, P.max_block, A + P.o_scratch, P.slot, e->d_xpow, e->nsm, s),
                "k_rle_dyn_blocks");                      // timed in the LZ77 slot
     R2P_CU(mark(4, defl && (P.any_lz || P.any_dyn)), "event");
-    if (defl) R2P_CU(launch_finalize(dimg, n, dblocks, e->d_xpow, s), "k_finalize");
+    if (defl) {
+        const int parts = finish_parts((int)P.nblk, e->nsm);
+        const int fgrid = (int)std::min<uint64_t>(P.nblk * (uint64_t)parts, (uint64_t)e->nsm * 8);
+        R2P_CU(launch_finish(dimg, dblocks, (int)P.nblk, parts, A + P.o_scratch, P.slot, e->d_xpow, fgrid, s),
+               "k_finish");
+    }
     R2P_CU(mark(5, defl), "event");
-    if (defl && (P.any_lz || P.any_dyn))
-        R2P_CU(launch_copy_blocks(dimg, dblocks, (int)P.nblk, A + P.o_scratch, P.slot, bgrid, s), "k_copy_blocks");
-    R2P_CU(mark(6, defl && (P.any_lz || P.any_dyn)), "event");
+    R2P_CU(mark(6, false), "event");   // the block gather runs inside k_finish
     return R2P_OK;
 }
 
@@ -481,8 +485,8 @@ int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stage
 void note_launch_graph(const Prepared& P)
 {
     const bool lz = P.any_lz, dyn = P.any_dyn;
-    const uint32_t n = (P.items.empty() ? 0u : 2u) + (P.ritems.empty() ? 0u : 1u) + 1u /* finalize */ +
-                       (P.any_stored ? 1u : 0u) + (lz ? 1u : 0u) + (dyn ? 1u : 0u) + ((lz || dyn) ? 1u : 0u);
+    const uint32_t n = (P.items.empty() ? 0u : 2u) + (P.ritems.empty() ? 0u : 1u) + 1u /* finish */ +
+                       (P.any_stored ? 1u : 0u) + (lz ? 1u : 0u) + (dyn ? 1u : 0u);
     g_launches.fetch_add(n, std::memory_order_relaxed);
 }
 

@@ -36,9 +36,10 @@ cudaError_t launch_window_filter_reg(DevImage* imgs, const BandItem* items, int 
 int stored_smem_bytes(int block_size);
 cudaError_t launch_stored(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block,
                           const uint32_t* xpow, int grid, cudaStream_t s);
-cudaError_t launch_finalize(DevImage* imgs, int nimg, BlockOut* blocks, const uint32_t* xpow, cudaStream_t s);
-cudaError_t launch_copy_blocks(const DevImage* imgs, const BlockOut* blocks, int nblocks,
-                               const uint8_t* scratch, uint64_t slot_bytes, int grid, cudaStream_t s);
+// k_finish over nblocks * parts units (slices of blocks) on `grid` CTAs
+cudaError_t launch_finish(DevImage* imgs, BlockOut* blocks, int nblocks, int parts, const uint8_t* scratch,
+                          uint64_t slot_bytes, const uint32_t* xpow, int grid, cudaStream_t s);
+int finish_parts(int nblocks, int nsm);   // slices per block for a launch of nblocks blocks
 size_t checksum_scratch_bytes(uint64_t len);
 cudaError_t launch_checksum(const uint8_t* data, uint64_t len, bool adler, uint32_t* result, void* scratch,
                             const uint32_t* xpow, int grid, cudaStream_t s);

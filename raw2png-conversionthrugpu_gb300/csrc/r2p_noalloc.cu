@@ -189,11 +189,9 @@ extern "C" int r2p_zlib_compress_noalloc(const void* d_in, size_t len, int level
     else if (level == 1) e = launch_lz77(dimg, dblk, (int)nb, bs, slots, slot, xpow, grid, 10, s);
     else e = launch_dyn(dimg, dblk, (int)nb, bs, slots, slot, xpow, nd.nsm, s);
     if (e != cudaSuccess) return na_fail(e, "DEFLATE blocks");
-    e = launch_finalize(dimg, 1, dblk, xpow, s);
-    if (e != cudaSuccess) return na_fail(e, "k_finalize");
-    if (level > 0) {
-        e = launch_copy_blocks(dimg, dblk, (int)nb, slots, slot, grid, s);
-        if (e != cudaSuccess) return na_fail(e, "k_copy_blocks");
-    }
+    const int parts = finish_parts((int)nb, nd.nsm);
+    const int fgrid = (int)std::min<size_t>(nb * (size_t)parts, (size_t)nd.nsm * 8);
+    e = launch_finish(dimg, dblk, (int)nb, parts, slots, slot, xpow, fgrid, s);
+    if (e != cudaSuccess) return na_fail(e, "k_finish");
     return R2P_OK;
 }
