@@ -20,7 +20,9 @@
 // head of a 3-byte hash table shared by the 32 lanes of a warp (seeded from
 // the ~2 KB before the warp's range); a match is taken when it is at least 4
 // bytes long, or 3 within 4096 bytes back (where its code, at most 22 bits,
-// is shorter than three literals).  The PNG filter has already taken the
+// is shorter than three literals).  A thread steps two positions at a time
+// (a match, a literal and a match, or two literals), which halves the steps
+// of the literal-heavy lanes a warp waits for.  The PNG filter has already taken the
 // scanline above out of the bytes, so a third candidate one scanline up found
 // almost nothing the hash did not (990 of 12.55 M bytes on a 3072x3072 16-bit
 // image) and cost a tenth of the launch; it is not searched.
@@ -101,20 +103,20 @@ __device__ __forceinline__ uint32_t hash3(uint32_t v, int hb) { return ((v & 0xF
 // a 64 KB block; 11 bits would not).
 __device__ __forceinline__ int lz_hash_bits(const DevImage& d) { return d.hash_bits == 9 ? 9 : 10; }
 
-// Fixed-Huffman code of a literal byte: reversed code and its length.
+// Fixed-Huffman code of a literal byte (RFC 1951 3.2.6): 0-143 are the 8-bit
+// codes 0x30.., 144-255 the 9-bit codes 0x190..; reversed for LSB-first
+// packing.  2b + 0x60 is 0x30 + b one bit up, so both reverse with >> 23.
 __device__ __forceinline__ void lit_code(uint32_t b, uint32_t& v, int& n)
 {
-    if (b < 144) { v = __brev(0x30u + b) >> 24; n = 8; }
-    else         { v = __brev(0x190u + b - 144u) >> 23; n = 9; }
+    const bool nine = b >= 144u;
+    v = __brev(nine ? b + 0x100u : 2u * b + 0x60u) >> 23;
+    n = 8 + (int)nine;
 }
 
-// Code tables for matches (RFC 1951 3.2.5-3.2.6), built per CTA in shared
-// memory from the definitions below:
-//   length entry  [len - 3]           reversed code | bits << 8 | extra bits << 12 | base (len - 3) << 16
-//   distance entry [d < 256 ? d : 256 + (d >> 7)], d = distance - 1
-//                                     reversed 5-bit code | extra bits << 8 | base d << 12
-// (for d >= 256 a code has >= 7 extra bits, so d >> 7 fixes the code).
-constexpr int kLenTab = 256, kDistTab = 512;
+// Length codes for matches (RFC 1951 3.2.5-3.2.6), built per CTA in shared
+// memory: entry [len - 3] = the reversed length code with its extra bits
+// above it (low 16 bits) | the total bit count << 16.
+constexpr int kLenTab = 256;
 
 __device__ uint32_t len_entry(int len)
 {
@@ -133,135 +135,150 @@ __device__ uint32_t len_entry(int len)
     int cl;
     if (sym <= 279) { code = __brev((uint32_t)(sym - 256)) >> 25; cl = 7; }
     else            { code = __brev((uint32_t)(0xC0 + sym - 280)) >> 24; cl = 8; }
-    return code | ((uint32_t)cl << 8) | ((uint32_t)lne << 12) | ((uint32_t)base << 16);
+    return (code | ((uint32_t)(l - base) << cl)) | ((uint32_t)(cl + lne) << 16);
 }
 
-__device__ uint32_t dist_entry(int i)
+// Code of a match: length entry `le` (from the table), distance D >= 1 coded
+// in place -- d = D - 1 below 4 is its own 5-bit code, otherwise the code is
+// 2 * e + 2 + the bit below the top one, with e = floor(log2 d) - 1 extra
+// bits (RFC 1951 3.2.5).  Returns the bits; *n gets their count (<= 31).
+__device__ __forceinline__ uint32_t match_code(uint32_t le, uint32_t D, int& n)
 {
-    const int d = i < 256 ? i : (i - 256) << 7;
-    int dc, dne, base;
-    if (d < 4) { dc = d; dne = 0; base = d; }
-    else {
-        const int lg = 31 - __clz(d);
-        dne = lg - 1;
-        dc = 2 * dne + 2 + ((d >> dne) & 1);
-        base = d & ~((1 << dne) - 1);
+    const uint32_t d = D - 1u;
+    const int lg = 31 - __clz((int)(d | 1u));
+    const int dne = d < 4u ? 0 : lg - 1;
+    const uint32_t dc = d < 4u ? d : (uint32_t)(2 * dne + 2) + ((d >> dne) & 1u);
+    const uint32_t dx = d & ((1u << dne) - 1u);
+    const int ln = (int)(le >> 16);
+    n = ln + 5 + dne;
+    return (le & 0xFFFFu) | (((__brev(dc) >> 27) | (dx << 5)) << ln);
+}
+
+// Append n <= 32 bits to the thread's LSB-first bit accumulator; whole words
+// go to its buffer `ob`.
+__device__ __forceinline__ void put_bits(uint64_t& acc, int& nacc, int& nw, uint32_t* ob, uint32_t v, int n)
+{
+    acc |= (uint64_t)v << nacc;
+    nacc += n;
+    if (nacc >= 32) {
+        ob[nw++] = (uint32_t)acc;
+        acc >>= 32;
+        nacc -= 32;
     }
-    return (__brev((uint32_t)dc) >> 27) | ((uint32_t)dne << 8) | ((uint32_t)base << 12);
 }
 
-// Length/distance pair -> packed bits (length code, extra, 5-bit distance code, extra).
-__device__ __forceinline__ void match_code(int len, int dist, const uint32_t* lt, const uint32_t* dt, uint32_t& v,
-                                           int& n)
+// Match candidates at position p (bytes w = p..p+3, the byte before = prev,
+// hash-head entry t): a run (distance 1) of 4 or more, the hash head with 4
+// or more equal bytes, a run of exactly 3, or the hash head with 3 equal
+// bytes within kFar3.  L = 4 means "at least 4: extend", 3 exactly 3, 0 none.
+__device__ __forceinline__ void match_at(const uint8_t* in, int p, int e, uint32_t w, uint32_t prev, int t, int& L,
+                                         int& D)
 {
-    const uint32_t le = lt[len - 3];
-    const uint32_t cl = (le >> 8) & 15u, lne = (le >> 12) & 15u;
-    const uint32_t lex = (uint32_t)(len - 3) - (le >> 16);
-    const int d = dist - 1;
-    const uint32_t de = dt[d < 256 ? d : 256 + (d >> 7)];
-    const uint32_t dne = (de >> 8) & 15u;
-    const uint32_t dex = (uint32_t)d - (de >> 12);
-    v = (le & 0xFFu) | (lex << cl) | ((de & 31u) << (cl + lne)) | (dex << (cl + lne + 5));
-    n = (int)(cl + lne + 5 + dne);
+    const uint32_t rx = w ^ (prev * 0x01010101u);
+    const int dist = p - (t - 1);              // <= 0: a later position of another lane, or empty
+    const uint32_t hx = dist > 0 ? (ld32u(in, t - 1) ^ w) : 1u;
+    L = 0;
+    D = 0;
+    if (rx == 0u) { D = 1; L = 4; }
+    else if (hx == 0u) { D = dist; L = 4; }
+    else if ((rx & 0xFFFFFFu) == 0u) { D = 1; L = 3; }
+    else if ((hx & 0xFFFFFFu) == 0u && dist <= kFar3) { D = dist; L = 3; }
+    if (p + 4 > e) L = 0;                      // a match must leave its 4 bytes inside the sub-range
 }
 
-// Greedy parse of in[s, e) by one thread into the word buffer `ob`.
-// `tab` is the warp's shared hash table (latest position + 1 per hash;
-// 0xFFFF when empty, a position no candidate can precede).
+// Length of a match of at least 4 bytes at ps, distance D, up to the
+// sub-range end e (and 258): runs by aligned words against the repeated byte
+// `rb`, other matches by unaligned word compares, then bytes.
+__device__ __forceinline__ int extend_match(const uint8_t* in, int ps, int e, int D, uint32_t rb)
+{
+    const uint32_t* W = reinterpret_cast<const uint32_t*>(in);
+    const int maxl = min(kMaxMatch, e - ps);
+    if (D == 1) {
+        const uint32_t rep = rb * 0x01010101u;
+        const int i = ps + 4, lim = ps + maxl;
+        int q = i >> 2;
+        uint32_t x = (W[q] ^ rep) & (0xFFFFFFFFu << (8 * (i & 3)));
+        while (!x && 4 * q + 4 < lim) x = W[++q] ^ rep;
+        const int end = x ? 4 * q + ((__ffs(x) - 1) >> 3) : 4 * q + 4;
+        return min(end, lim) - ps;
+    }
+    const int c = ps - D;
+    int L = 4;
+    bool more = true;
+    while (more && L + 4 <= maxl) {
+        const uint32_t x = ld32u(in, c + L) ^ ld32u(in, ps + L);
+        if (x) { L += (__ffs(x) - 1) >> 3; more = false; }
+        else L += 4;
+    }
+    while (more && L < maxl && in[c + L] == in[ps + L]) L++;
+    return L;
+}
+
+// Greedy parse of in[s, e) by one thread into the word buffer `ob`, two
+// positions per step: each step looks up (and enters into the warp's hash
+// table `tab`: latest position + 1 per hash, 0xFFFF when empty) positions p
+// and p+1, then emits a match at p, or a literal at p and a match at p+1, or
+// two literals.  A literal-heavy lane -- the one a warp waits for -- so takes
+// half as many steps, and literals and matches share one coding path (the
+// selects below), so the lanes of a warp only diverge in match extension.
+// Position p+1 enters the table even when a match at p covers it.
 // Returns the number of bits written; the last partial word is stored too.
-//
-// The thread keeps two sliding registers -- w (bytes p..p+3) and the byte
-// before p -- so a literal step reads one new byte.
 __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t* tab, uint32_t* ob,
-                               const uint32_t* lt, const uint32_t* dt)
+                               const uint32_t* lt)
 {
+    const uint32_t* W = reinterpret_cast<const uint32_t*>(in);
     uint64_t acc = 0;
     int nacc = 0, nw = 0;
     int p = s;
-    // sliding state for position p (bytes past the block end read the zero padding)
-    uint32_t w = ld32u(in, p);
-    // at the block start no run can match: a "previous byte" unequal to w's first byte
-    uint32_t prev = p > 0 ? (uint32_t)in[p - 1] : ((w & 0xFFu) ^ 1u);
+    // at the block start no run can match: a "previous byte" unequal to byte 0
+    const uint32_t prev0 = p > 0 ? (uint32_t)in[p - 1] : ((uint32_t)in[0] ^ 1u);
     while (p + 4 <= e) {
-        int L = 0, D = 0;
+        // bytes p-1 .. p+6 from three aligned words (bytes past the block end
+        // read the zero padding)
+        uint32_t wlo, whi;
         {
-            const uint32_t h = hash3(w, hb);
-            const int t = tab[h];
-            tab[h] = (uint16_t)(p + 1);
-            const uint32_t rx = w ^ (prev * 0x01010101u);
-            if (rx == 0u) {
-                D = 1;                              // a run of 4 or more
-            } else {
-                const int dist = p - (t - 1);       // <= 0: a later position of another lane, or empty
-                const uint32_t hx = dist > 0 ? (ld32u(in, t - 1) ^ w) : 1u;
-                if (hx == 0u) {
-                    D = dist;                       // 4 or more equal bytes
-                } else if ((rx & 0xFFFFFFu) == 0u) {
-                    L = 3;                          // a run of exactly 3
-                    D = 1;
-                } else if ((hx & 0xFFFFFFu) == 0u && dist <= kFar3) {
-                    L = 3;                          // 3 equal bytes, near enough to pay
-                    D = dist;
-                }
-            }
-            if (D && !L) {
-                // extend by words, then bytes, up to the sub-range end
-                const int maxl = min(kMaxMatch, e - p);
-                if (D == 1) {
-                    // a run: aligned words against the byte replicated
-                    const uint32_t rep = prev * 0x01010101u;
-                    const uint32_t* in32 = reinterpret_cast<const uint32_t*>(in);
-                    const int i = p + 4, lim = p + maxl;
-                    int q = i >> 2;
-                    uint32_t x = (in32[q] ^ rep) & (0xFFFFFFFFu << (8 * (i & 3)));
-                    while (!x && 4 * q + 4 < lim) x = in32[++q] ^ rep;
-                    const int end = x ? 4 * q + ((__ffs(x) - 1) >> 3) : 4 * q + 4;
-                    L = min(end, lim) - p;
-                } else {
-                    const int c = p - D;
-                    L = 4;
-                    bool more = true;
-                    while (more && L + 4 <= maxl) {
-                        const uint32_t x = ld32u(in, c + L) ^ ld32u(in, p + L);
-                        if (x) { L += (__ffs(x) - 1) >> 3; more = false; }
-                        else L += 4;
-                    }
-                    while (more && L < maxl && in[c + L] == in[p + L]) L++;
-                }
+            const int pm = max(p - 1, 0);
+            const int q = pm >> 2;
+            const uint32_t sh = (uint32_t)(pm & 3) << 3;
+            const uint32_t a = W[q], b = W[q + 1], c = W[q + 2];
+            wlo = __funnelshift_r(a, b, sh);
+            whi = __funnelshift_r(b, c, sh);
+            if (p == 0) {
+                whi = __funnelshift_l(wlo, whi, 8);
+                wlo = (wlo << 8) | prev0;
             }
         }
-        uint32_t v;
-        int nb;
-        if (L >= 3) {
-            match_code(L, D, lt, dt, v, nb);
-            p += L;
-            w = ld32u(in, p);
-            prev = in[p - 1];
-        } else {
-            lit_code(w & 0xFFu, v, nb);
-            prev = w & 0xFFu;
-            w = (w >> 8) | ((uint32_t)in[p + 4] << 24);
-            p += 1;
-        }
-        acc |= (uint64_t)v << nacc;
-        nacc += nb;
-        if (nacc >= 32) {
-            ob[nw++] = (uint32_t)acc;
-            acc >>= 32;
-            nacc -= 32;
-        }
+        const uint32_t prev = wlo & 0xFFu;
+        const uint32_t w0 = __funnelshift_r(wlo, whi, 8);     // bytes p .. p+3
+        const uint32_t w1 = __funnelshift_r(wlo, whi, 16);    // bytes p+1 .. p+4
+        const uint32_t h0 = hash3(w0, hb);
+        const int t0 = tab[h0];
+        tab[h0] = (uint16_t)(p + 1);
+        const uint32_t h1 = hash3(w1, hb);
+        const int t1 = tab[h1];
+        if (p + 5 <= e) tab[h1] = (uint16_t)(p + 2);
+        int L0, D0, L1, D1;
+        match_at(in, p, e, w0, prev, t0, L0, D0);
+        match_at(in, p + 1, e, w1, w0 & 0xFFu, t1, L1, D1);
+        const bool m0 = L0 != 0, m1 = !m0 && L1 != 0;
+        const int ps = m0 ? p : p + 1;
+        const int D = m0 ? D0 : D1;
+        int L = m0 ? L0 : L1;
+        if (L == 4) L = extend_match(in, ps, e, D, m0 ? prev : (w0 & 0xFFu));
+        int mn, ln0, ln1;
+        const uint32_t mv = match_code(lt[(m0 || m1) ? L - 3 : 0], (m0 || m1) ? (uint32_t)D : 1u, mn);
+        uint32_t lv0, lv1;
+        lit_code(w0 & 0xFFu, lv0, ln0);
+        lit_code(w1 & 0xFFu, lv1, ln1);
+        put_bits(acc, nacc, nw, ob, m0 ? mv : lv0, m0 ? mn : ln0);
+        if (!m0) put_bits(acc, nacc, nw, ob, m1 ? mv : lv1, m1 ? mn : ln1);
+        p += m0 ? L : (m1 ? 1 + L : 2);
     }
     for (; p < e; p++) {                        // the last bytes: literals
         uint32_t v;
         int nb;
         lit_code(in[p], v, nb);
-        acc |= (uint64_t)v << nacc;
-        nacc += nb;
-        if (nacc >= 32) {
-            ob[nw++] = (uint32_t)acc;
-            acc >>= 32;
-            nacc -= 32;
-        }
+        put_bits(acc, nacc, nw, ob, v, nb);
     }
     if (nacc > 0) ob[nw] = (uint32_t)acc;
     return (uint32_t)(nw * 32 + nacc);
@@ -306,10 +323,9 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
     __shared__ uint32_t wsum[(NT / 32)], wa1[(NT / 32)], wa2[(NT / 32)];
     __shared__ uint32_t s_info[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    __shared__ uint32_t s_len[kLenTab], s_dist[kDistTab];
+    __shared__ uint32_t s_len[kLenTab];
     build_crc_tables(ctab);
     for (int i = threadIdx.x; i < kLenTab; i += NT) s_len[i] = len_entry(i + 3);
-    for (int i = threadIdx.x; i < kDistTab; i += NT) s_dist[i] = dist_entry(i);
     uint32_t* myout = outs + tid * lw;
 
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
@@ -352,7 +368,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         }
         // parse this thread's sub-range
         const int s = min(n, tid * sub), e = min(n, s + sub);
-        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, hb, mytab, myout, s_len, s_dist) : 0u;
+        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, hb, mytab, myout, s_len) : 0u;
         // Adler sums of the sub-range, taken while slower warps still parse:
         // S1 = sum d_i, S2 = sum (n - i) d_i mod 65521 (< 2^31 before the
         // reduction: at most 17 words of weight <= 65520)
@@ -382,12 +398,16 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         }
         if (lane == 31) { wsum[warp] = incl; wa1[warp] = a1; wa2[warp] = a2; }
         __syncthreads();
-        uint32_t wbase = 0, tot = 3;
-        for (int k = 0; k < (NT / 32); k++) {
-            if (k < warp) wbase += wsum[k];
-            tot += wsum[k];
+        // the warps' bases: lane k of every warp scans warp k's bit count
+        const uint32_t ws = lane < NT / 32 ? wsum[lane] : 0u;
+        uint32_t wx = ws;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, wx, o);
+            if (lane >= o) wx += y;
         }
-        tot += 7;                                                  // end-of-block code
+        const uint32_t wbase = __shfl_sync(FULL, wx - ws, warp);
+        const uint32_t tot = 3 + __shfl_sync(FULL, wx, 31) + 7;   // header, streams, end-of-block code
         const uint32_t off = 3 + wbase + incl - nbits;             // bit offset of this thread's stream
         if (tid == 0) {
             const uint32_t huff = last ? (tot + 7) / 8 : (tot + 3 + 7) / 8 + 4;
