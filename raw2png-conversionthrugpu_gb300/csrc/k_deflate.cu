@@ -228,14 +228,28 @@ k_finish(DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, int nblocks
         BlockOut* B = blocks + d.blk0;
         const int nb = d.nblocks, local = b - d.blk0;
         const int st0 = d.status;
-        uint64_t before = 0, all = 0;
-        for (int i = threadIdx.x; i < nb; i += NT) {
-            const uint64_t len = B[i].out_len;
-            all += len;
-            if (i < local) before += len;
+        // one warp sums the image's block lengths: this block's stream
+        // offset and the stream length
+        if (threadIdx.x < 32) {
+            uint64_t before = 0, all = 0;
+            for (int i = threadIdx.x; i < nb; i += 32) {
+                const uint64_t len = B[i].out_len;
+                all += len;
+                if (i < local) before += len;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                before += __shfl_xor_sync(0xFFFFFFFFu, before, o);
+                all += __shfl_xor_sync(0xFFFFFFFFu, all, o);
+            }
+            if (threadIdx.x == 0) {
+                sw[0] = before;
+                sw[1] = all;
+            }
         }
-        before = cta_sum64<NT>(before, red64);
-        all = cta_sum64<NT>(all, red64);
+        __syncthreads();
+        const uint64_t before = sw[0], all = sw[1];
+        __syncthreads();                         // sw is reused by the image finish and the next unit
         if (local == 0 && part == 0) {
             if (!have_tab) {
                 build_crc_tables(tab);

@@ -167,34 +167,50 @@ __device__ void cta_crc_adler(const uint8_t* buf, int n, bool want_adler, const 
 }
 
 // Copy n bytes from a 4-byte-aligned source (shared or global) to an
-// arbitrary global destination, 16-byte stores for the aligned interior.
+// arbitrary global destination that does not overlap it, 16-byte stores for
+// the aligned interior.  Each thread loads two chunks before it stores them,
+// so two load round trips are in flight per thread.
 template <int NT>
-__device__ void cta_copy_to_global(uint8_t* dst, const uint8_t* src, int n)
+__device__ void cta_copy_to_global(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src, int n)
 {
     if (n <= 0) return;
     const uintptr_t d0 = reinterpret_cast<uintptr_t>(dst);
     const uintptr_t a0 = (d0 + 15) & ~(uintptr_t)15;              // first aligned dst
     const uintptr_t a1 = (d0 + (uintptr_t)n) & ~(uintptr_t)15;    // end of aligned part
     const int head = (int)min((uintptr_t)n, a0 - d0);
-    const uint32_t* sw = reinterpret_cast<const uint32_t*>(src);
+    const uint32_t* __restrict__ sw = reinterpret_cast<const uint32_t*>(src);
     if (a1 > a0) {
         const int o0 = (int)(a0 - d0);                           // data index of first aligned byte
         const uint32_t sh = (uint32_t)(o0 & 3) << 3;
         const int nchunks = (int)((a1 - a0) >> 4);
-        for (int c = threadIdx.x; c < nchunks; c += NT) {
-            const int o = o0 + 16 * c;
-            const int q = o >> 2;
-            uint32_t v[5];
+        // chunk c: source words q..q+4 (word q+4 holds bytes needed when the
+        // shift is non-zero; it is loaded whenever it contains a valid byte,
+        // so the copy never reads past that word)
+        auto load = [&](int c, uint32_t* v) {
+            const int q = (o0 + 16 * c) >> 2;
             v[0] = sw[q]; v[1] = sw[q + 1]; v[2] = sw[q + 2]; v[3] = sw[q + 3];
-            // word q+4 holds bytes needed when the shift is non-zero; load it
-            // whenever it contains a valid byte (never reads past that word)
             v[4] = (4 * (q + 4) < n) ? sw[q + 4] : 0u;
+        };
+        auto store = [&](int c, const uint32_t* v) {
             uint4 o4;
             o4.x = fshr(v[0], v[1], sh);
             o4.y = fshr(v[1], v[2], sh);
             o4.z = fshr(v[2], v[3], sh);
             o4.w = fshr(v[3], v[4], sh);
             *reinterpret_cast<uint4*>(a0 + 16 * (uintptr_t)c) = o4;
+        };
+        int c = threadIdx.x;
+        for (; c + NT < nchunks; c += 2 * NT) {
+            uint32_t v[5], u[5];
+            load(c, v);
+            load(c + NT, u);
+            store(c, v);
+            store(c + NT, u);
+        }
+        if (c < nchunks) {
+            uint32_t v[5];
+            load(c, v);
+            store(c, v);
         }
         const int tail0 = (int)(a1 - d0);
         for (int i = threadIdx.x; i < head; i += NT) dst[i] = src[i];

@@ -216,12 +216,11 @@ __device__ __forceinline__ int extend_match(const uint8_t* in, int ps, int e, in
 
 // Greedy parse of in[s, e) by one thread into the word buffer `ob`, two
 // positions per step: each step looks up (and enters into the warp's hash
-// table `tab`: latest position + 1 per hash, 0xFFFF when empty) positions p
-// and p+1, then emits a match at p, or a literal at p and a match at p+1, or
-// two literals.  A literal-heavy lane -- the one a warp waits for -- so takes
+// table `tab`: latest position + 1 per hash, 0xFFFF when empty) position p,
+// and p+1 when p is a literal, then emits a match at p, or a literal at p
+// and a match at p+1, or two literals.  A literal-heavy lane -- the one a warp waits for -- so takes
 // half as many steps, and literals and matches share one coding path (the
 // selects below), so the lanes of a warp only diverge in match extension.
-// Position p+1 enters the table even when a match at p covers it.
 // Returns the number of bits written; the last partial word is stored too.
 __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t* tab, uint32_t* ob,
                                const uint32_t* lt)
@@ -254,13 +253,16 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t
         const uint32_t h0 = hash3(w0, hb);
         const int t0 = tab[h0];
         tab[h0] = (uint16_t)(p + 1);
-        const uint32_t h1 = hash3(w1, hb);
-        const int t1 = tab[h1];
-        if (p + 5 <= e) tab[h1] = (uint16_t)(p + 2);
-        int L0, D0, L1, D1;
+        int L0, D0, L1 = 0, D1 = 0;
         match_at(in, p, e, w0, prev, t0, L0, D0);
-        match_at(in, p + 1, e, w1, w0 & 0xFFu, t1, L1, D1);
-        const bool m0 = L0 != 0, m1 = !m0 && L1 != 0;
+        const bool m0 = L0 != 0;
+        if (!m0) {                                // p+1 is looked up (and entered) only if p is a literal
+            const uint32_t h1 = hash3(w1, hb);
+            const int t1 = tab[h1];
+            if (p + 5 <= e) tab[h1] = (uint16_t)(p + 2);
+            match_at(in, p + 1, e, w1, w0 & 0xFFu, t1, L1, D1);
+        }
+        const bool m1 = !m0 && L1 != 0;
         const int ps = m0 ? p : p + 1;
         const int D = m0 ? D0 : D1;
         int L = m0 ? L0 : L1;
