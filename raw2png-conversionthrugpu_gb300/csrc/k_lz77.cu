@@ -169,8 +169,8 @@ __device__ __forceinline__ void put_bits(uint64_t& acc, int& nacc, int& nw, uint
 
 // Match candidates at position p (bytes w = p..p+3, the byte before = prev,
 // hash-head entry t): a run (distance 1) of 4 or more, the hash head with 4
-// or more equal bytes, a run of exactly 3, or the hash head with 3 equal
-// bytes within kFar3.  L = 4 means "at least 4: extend", 3 exactly 3, 0 none.
+// or more equal bytes, or the hash head with 3 equal bytes within kFar3.
+// L = 4 means "at least 4: extend", 3 exactly 3, 0 none.
 __device__ __forceinline__ void match_at(const uint8_t* in, int p, int e, uint32_t w, uint32_t prev, int t, int& L,
                                          int& D)
 {
@@ -181,7 +181,6 @@ __device__ __forceinline__ void match_at(const uint8_t* in, int p, int e, uint32
     D = 0;
     if (rx == 0u) { D = 1; L = 4; }
     else if (hx == 0u) { D = dist; L = 4; }
-    else if ((rx & 0xFFFFFFu) == 0u) { D = 1; L = 3; }
     else if ((hx & 0xFFFFFFu) == 0u && dist <= kFar3) { D = dist; L = 3; }
     if (p + 4 > e) L = 0;                      // a match must leave its 4 bytes inside the sub-range
 }
@@ -218,10 +217,18 @@ __device__ __forceinline__ int extend_match(const uint8_t* in, int ps, int e, in
 // positions per step: each step looks up (and enters into the warp's hash
 // table `tab`: latest position + 1 per hash, 0xFFFF when empty) position p,
 // and p+1 when p is a literal, then emits a match at p, or a literal at p
-// and a match at p+1, or two literals.  A literal-heavy lane -- the one a warp waits for -- so takes
-// half as many steps, and literals and matches share one coding path (the
-// selects below), so the lanes of a warp only diverge in match extension.
+// and a match at p+1, or two literals.  A literal-heavy lane -- the one a
+// warp waits for -- so takes half as many steps, and literals and matches
+// share one coding path (the selects below), so the lanes of a warp only
+// diverge in match extension.
+// Every lane of the warp calls it (lanes with nothing to parse too): after
+// kProbeSteps steps the warp votes, and if its lanes' codes so far take 8 or
+// more bits per input byte -- no better than stored bytes, as on noise --
+// the warp codes the rest of its range as plain literals, skipping the
+// match search.  The vote depends on the block's bytes alone.
 // Returns the number of bits written; the last partial word is stored too.
+constexpr int kProbeSteps = 8;
+
 __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t* tab, uint32_t* ob,
                                const uint32_t* lt)
 {
@@ -231,7 +238,7 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t
     int p = s;
     // at the block start no run can match: a "previous byte" unequal to byte 0
     const uint32_t prev0 = p > 0 ? (uint32_t)in[p - 1] : ((uint32_t)in[0] ^ 1u);
-    while (p + 4 <= e) {
+    auto step = [&]() {
         // bytes p-1 .. p+6 from three aligned words (bytes past the block end
         // read the zero padding)
         uint32_t wlo, whi;
@@ -275,7 +282,12 @@ __device__ uint32_t parse_lane(const uint8_t* in, int s, int e, int hb, uint16_t
         put_bits(acc, nacc, nw, ob, m0 ? mv : lv0, m0 ? mn : ln0);
         if (!m0) put_bits(acc, nacc, nw, ob, m1 ? mv : lv1, m1 ? mn : ln1);
         p += m0 ? L : (m1 ? 1 + L : 2);
-    }
+    };
+    for (int k = 0; k < kProbeSteps && p + 4 <= e; k++) step();
+    const uint32_t wbits = __reduce_add_sync(FULL, (uint32_t)(nw * 32 + nacc));
+    const uint32_t wbytes = __reduce_add_sync(FULL, (uint32_t)(p - s));
+    if (wbits < 8u * wbytes || wbytes == 0u)
+        while (p + 4 <= e) step();
     for (; p < e; p++) {                        // the last bytes: literals
         uint32_t v;
         int nb;
@@ -370,7 +382,7 @@ k_lz77_blocks(const DevImage* __restrict__ imgs, BlockOut* __restrict__ blocks, 
         }
         // parse this thread's sub-range
         const int s = min(n, tid * sub), e = min(n, s + sub);
-        const uint32_t nbits = (s < e) ? parse_lane(in, s, e, hb, mytab, myout, s_len) : 0u;
+        const uint32_t nbits = parse_lane(in, s, e, hb, mytab, myout, s_len);
         // Adler sums of the sub-range, taken while slower warps still parse:
         // S1 = sum d_i, S2 = sum (n - i) d_i mod 65521 (< 2^31 before the
         // reduction: at most 17 words of weight <= 65520)
