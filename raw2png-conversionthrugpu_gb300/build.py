@@ -15,7 +15,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libr2p.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_SOURCES = ["k_filter.cu", "k_filter_reg.cu", "k_deflate.cu", "k_lz77.cu", "r2p_engine.cu", "r2p_batch.cu",
+CU_SOURCES = ["k_filter.cu", "k_filter_reg.cu", "k_filter_rows.cu", "k_deflate.cu", "k_lz77.cu", "r2p_engine.cu", "r2p_batch.cu",
               "r2p_server.cu", "r2p_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",

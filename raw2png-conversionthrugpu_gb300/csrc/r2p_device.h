@@ -32,12 +32,20 @@ enum BmpKind : int {
 // Largest table kept in shared memory by the filter kernel (bytes).
 constexpr int kMaxSmemLut = 32768;
 
+// Window+filter kernel an image's rows go to (DevImage::fpath).
+enum FiltPath : int {
+    kFiltSmem = 0,    // k_window_filter: TMA-staged tiles in shared memory
+    kFiltReg = 1,     // k_window_filter_reg: a row across a group of warps' registers
+    kFiltRows = 2,    // k_filter_rows: one warp per row, table built by k_window_lut
+};
+
 struct DevImage {
     // geometry
     uint32_t width, height;
     int32_t channels, ib, ob;       // input / output bytes per sample
     int32_t rb, bpp;                // filtered row bytes (without type byte), bytes per pixel
     int32_t in_pitch;               // raw bytes per row
+    int32_t fpath;                  // FiltPath: the kernel that filters this image's rows
     uint64_t filt_bytes;            // height * (rb + 1)
     // window request and its resolution (filled on the device)
     int32_t req_mode;               // R2P_WINDOW_*

@@ -176,6 +176,7 @@ int plan_image(const r2p_image& im, int out_kind, ImgPlan& ip, const std::vector
     ip.reg_lut = entries * esize;
     ip.reg = reg_filter_eligible(d.rb, d.in_pitch, ip.reg_lut);
     ip.reg_w = reg_filter_warps(d.rb);
+    ip.rows = d.rb >= kRowsMinRowBytes && rows_filter_eligible(d.in_pitch, ip.reg_lut);
     ip.png_bound = (uint64_t)d.prefix + F + (uint64_t)kStoredHdr * nb + (out_kind == 0 ? kPngSuffix : 4);
     if (F >= (1ull << 32) || ip.png_bound >= (1ull << 31) - 64)
         return set_err(R2P_EINVAL, "image too large for a single IDAT chunk");
@@ -280,14 +281,34 @@ void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb
     std::vector<char> use_reg((size_t)n, 0);
     int max_w = 0, nreg = 0;
     for (int i = 0; i < n; i++) {
-        use_reg[(size_t)i] = plans[i].reg && plans[i].smem > 0 && i < (int)cb.raw.size() &&
-                             (reinterpret_cast<uintptr_t>(cb.raw[i]) & 15) == 0;
+        const bool aligned = i < (int)cb.raw.size() && (reinterpret_cast<uintptr_t>(cb.raw[i]) & 15) == 0;
+        if (plans[i].rows && aligned) {
+            // wide rows: one warp per row, items of whole CTAs' worth of rows
+            plans[i].di.fpath = kFiltRows;
+            P.wlut = std::max(P.wlut, plans[i].reg_lut);
+            const DevImage& d = plans[i].di;
+            const uint64_t rows = (uint64_t)rows_filter_rows_per_item();
+            for (uint64_t r = 0; r < d.height; r += rows)
+                P.witems.push_back(BandItem{(uint32_t)i, (uint32_t)r, (uint32_t)std::min<uint64_t>(d.height, r + rows)});
+            continue;
+        }
+        use_reg[(size_t)i] = plans[i].reg && plans[i].smem > 0 && aligned;
+        plans[i].di.fpath = use_reg[(size_t)i] ? kFiltReg : kFiltSmem;
         if (use_reg[(size_t)i]) {
             max_w = std::max(max_w, plans[i].reg_w);
             nreg++;
         } else {
             P.smem = std::max(P.smem, plans[i].smem);
         }
+    }
+    if (!P.witems.empty()) {
+        // one stash size per launch: the largest any of its images can use
+        // (an image whose rows need more is windowed again in pass 2)
+        for (int i = 0; i < n; i++)
+            if (plans[i].di.fpath == kFiltRows)
+                P.wstash = std::max(P.wstash, rows_filter_stash(plans[i].di.rb, P.wlut));
+        P.wsmem = rows_filter_smem(P.wlut, P.wstash);
+        P.wslots = e->nsm * rows_filter_ctas_per_sm(P.wsmem);
     }
     const int cps = P.smem > 0 ? filter_ctas_per_sm(P.smem) : 1;
     P.slots_total = e->nsm * cps;
@@ -333,7 +354,7 @@ void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb
         P.items.clear();
         if (P.smem <= 0) return;
         for (int i = 0; i < n; i++) {
-            if (use_reg[(size_t)i]) continue;
+            if (plans[i].di.fpath != kFiltSmem) continue;    // another kernel filters this image
             const DevImage& d = plans[i].di;
             const int T = filter_tile_rows(d.rb, d.in_pitch, P.smem, plans[i].lreg);
             const uint64_t ntiles = (d.height + T - 1) / T;
@@ -385,6 +406,7 @@ void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb
     P.o_img = L.take(sizeof(DevImage) * n);
     P.o_items = L.take(sizeof(BandItem) * std::max<size_t>(1, P.items.size()));
     P.o_ritems = L.take(sizeof(BandItem) * std::max<size_t>(1, P.ritems.size()));
+    P.o_witems = L.take(sizeof(BandItem) * std::max<size_t>(1, P.witems.size()));
     P.o_blocks = L.take(sizeof(BlockOut) * std::max<size_t>(1, P.blocks.size()));
     P.desc_bytes = L.off;
     P.o_lut = L.take(lut_total);
@@ -422,6 +444,7 @@ void write_descriptors(uint8_t* H, const std::vector<ImgPlan>& plans, const Prep
     for (size_t i = 0; i < plans.size(); i++) memcpy(H + P.o_img + i * sizeof(DevImage), &plans[i].di, sizeof(DevImage));
     if (!P.items.empty()) memcpy(H + P.o_items, P.items.data(), P.items.size() * sizeof(BandItem));
     if (!P.ritems.empty()) memcpy(H + P.o_ritems, P.ritems.data(), P.ritems.size() * sizeof(BandItem));
+    if (!P.witems.empty()) memcpy(H + P.o_witems, P.witems.data(), P.witems.size() * sizeof(BandItem));
     if (!P.blocks.empty()) memcpy(H + P.o_blocks, P.blocks.data(), P.blocks.size() * sizeof(BlockOut));
 }
 
@@ -441,6 +464,7 @@ int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stage
     };
     const bool filt = (stages & ST_FILTER) != 0, defl = (stages & ST_DEFLATE) != 0, bmp = (stages & ST_BMP) != 0;
     const bool old_filt = filt && !P.items.empty(), reg_filt = filt && !P.ritems.empty();
+    const bool rows_filt = filt && !P.witems.empty();
     R2P_CU(mark(0, false), "event");
     // window tables in HBM: only the shared-memory filter kernel and the BMP
     // export read them (the register kernel builds its table per CTA)
@@ -455,6 +479,12 @@ int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stage
         const int grid = (int)std::min<size_t>(P.ritems.size(), (size_t)P.rslots);
         R2P_CU(launch_window_filter_reg(dimg, dritems, (int)P.ritems.size(), grid, P.rnw, P.rsmem, s),
                "k_window_filter_reg");
+    }
+    if (rows_filt) {
+        BandItem* dwitems = reinterpret_cast<BandItem*>(A + P.o_witems);
+        const int grid = (int)std::min<size_t>(P.witems.size(), (size_t)P.wslots);
+        R2P_CU(launch_filter_rows(dimg, n, P.wlut, P.wstash, dwitems, (int)P.witems.size(), grid, s),
+               "k_filter_rows");
     }
     if (bmp) R2P_CU(launch_bmp(dimg, n, P.bmp_words, e->nsm, s), "k_bmp_file");   // timed in the filter's slot
     R2P_CU(mark(2, filt || bmp), "event");
@@ -485,7 +515,8 @@ int launch_stages(r2p_engine* e, int n, const Prepared& P, uint8_t* A, int stage
 void note_launch_graph(const Prepared& P)
 {
     const bool lz = P.any_lz, dyn = P.any_dyn;
-    const uint32_t n = (P.items.empty() ? 0u : 2u) + (P.ritems.empty() ? 0u : 1u) + 1u /* finish */ +
+    const uint32_t n = (P.items.empty() ? 0u : 2u) + (P.ritems.empty() ? 0u : 1u) + (P.witems.empty() ? 0u : 2u) +
+                       1u /* finish */ +
                        (P.any_stored ? 1u : 0u) + (lz ? 1u : 0u) + (dyn ? 1u : 0u);
     g_launches.fetch_add(n, std::memory_order_relaxed);
 }

@@ -41,7 +41,13 @@ struct ImgPlan {
     bool reg = false;  // rows fit the register-resident filter kernel (k_filter_reg.cu)
     int reg_w = 0;     // its warps per row
     int reg_lut = 0;   // its worst-case window table bytes
+    bool rows = false; // rows wide enough for the warp-per-row filter kernel (k_filter_rows.cu)
 };
+
+// Rows at least this wide (filtered bytes) go to the warp-per-row filter
+// kernel; narrower ones to the register-group kernel, where a row fills only
+// part of a warp's 512 bytes per step anyway.
+constexpr int kRowsMinRowBytes = 4096;
 
 // Built-in size-class table (the autotuner's GB300 result).
 extern const std::vector<r2p_tuning> kDefaultTuning;
@@ -153,13 +159,16 @@ static int ensure_stage(r2p_engine* e, size_t need, int* slot)
 struct Prepared {
     std::vector<BandItem> items;       // bands of the shared-memory filter kernel
     std::vector<BandItem> ritems;      // bands of the register-resident filter kernel
+    std::vector<BandItem> witems;      // bands of the warp-per-row filter kernel
     std::vector<BlockOut> blocks;
     int smem = 0, slots_total = 0, max_block = 0;
     int rnw = 0, rsmem = 0, rslots = 0;   // register kernel: warps per CTA, shared memory, CTA slots
+    int wsmem = 0, wslots = 0, wlut = 0;  // warp-per-row kernel: shared memory, CTA slots, largest table
+    int wstash = 0;                       // its per-warp stash of windowed rows (bytes; 0 = none)
     uint32_t nblk = 0;
     bool any_lz = false, any_stored = false, any_dyn = false;
     uint64_t slot = 0;
-    size_t o_img = 0, o_items = 0, o_ritems = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0,
+    size_t o_img = 0, o_items = 0, o_ritems = 0, o_witems = 0, o_blocks = 0, desc_bytes = 0, o_lut = 0, o_filt = 0, o_scratch = 0,
            o_extra = 0;
     size_t total = 0;
     int hash_bits = 10;

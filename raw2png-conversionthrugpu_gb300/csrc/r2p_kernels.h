@@ -32,6 +32,17 @@ int reg_filter_ctas_per_sm(int nw, int smem);
 cudaError_t launch_window_filter_reg(DevImage* imgs, const BandItem* items, int nitems, int grid, int nw, int smem,
                                      cudaStream_t s);
 
+// k_filter_rows.cu: wide rows, one warp per row; k_window_lut builds the
+// tables of the images whose fpath is kFiltRows, then k_filter_rows runs
+// over items of rows_filter_rows_per_item() rows
+bool rows_filter_eligible(int in_pitch, int lut_bytes);
+int rows_filter_rows_per_item();
+int rows_filter_stash(int rb, int lut_bytes);       // per-warp stash bytes for such rows (0: none)
+int rows_filter_smem(int lut_bytes, int stash);
+int rows_filter_ctas_per_sm(int smem);
+cudaError_t launch_filter_rows(DevImage* imgs, int n, int lut_bytes, int stash, const BandItem* items, int nitems,
+                               int grid, cudaStream_t s);
+
 // k_deflate.cu
 int stored_smem_bytes(int block_size);
 cudaError_t launch_stored(const DevImage* imgs, BlockOut* blocks, int nblocks, int max_block,
