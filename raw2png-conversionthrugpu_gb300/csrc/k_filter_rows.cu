@@ -50,7 +50,7 @@ namespace r2p {
 constexpr int kRowsWarps = 8;                  // warps per CTA: rows filtered side by side
 constexpr int kRowsThreads = 32 * kRowsWarps;
 constexpr int kRowsLutMax = 32768;             // table bytes a CTA keeps in shared memory
-constexpr int kRowsSmemMax = 113 * 1024;       // dynamic shared memory of a CTA: two fit an SM
+constexpr int kRowsSmemMax = 74 * 1024;        // dynamic shared memory of a CTA: three fit an SM
 constexpr int kLutEntriesPerCta = 1024;        // k_window_lut: four entries per thread
 
 // Everything a warp needs about its image, in registers.
@@ -275,21 +275,22 @@ __device__ __forceinline__ void emit_row(const WinCtx& w, const RowsJob& J, int 
     }
 }
 
-// Bytes of a warp's stash for rows of nch chunks: row j's windowed bytes
-// and the row above, each behind 16 zero bytes (what lies left of the row
-// start), so that pass 2 reads them back instead of windowing again.
-__host__ __device__ inline int rows_stash_bytes(int nch) { return 32 + 1024 * nch; }
+// One stashed row of nch chunks: its windowed bytes behind 16 zero bytes
+// (what lies left of the row start).  A CTA's stash holds kRowsWarps + 1 of
+// them: slot 0 the row above the item's first row, slot 1 + w warp w's row,
+// so the row above warp w's row is slot w, written by the warp before it.
+__host__ __device__ inline int rows_slot_bytes(int nch) { return 16 + 512 * nch; }
+__host__ __device__ inline int rows_stash_bytes(int nch) { return (kRowsWarps + 1) * rows_slot_bytes(nch); }
 
-// Pass 2 for filter F from the warp's stash xs (row j at xs + 16, the row
-// above at xs + 32 + 512 nch).
+// Pass 2 for filter F from the stash: row j's windowed bytes at xrow, the
+// row above at brow (each with 16 zero bytes before it).
 template <int DW, int F>
-__device__ __forceinline__ void emit_stash(const RowsJob& J, int j, int lane, const uint8_t* xs)
+__device__ __forceinline__ void emit_stash(const RowsJob& J, int j, int lane, const uint8_t* xrow,
+                                           const uint8_t* brow)
 {
     uint8_t* R = J.filt + (size_t)j * (size_t)(J.rb + 1);
     if (lane == 0) R[0] = (uint8_t)F;
     const bool keep_last = J.last_row != nullptr && j == J.height - 1;
-    const uint8_t* xrow = xs + 16;
-    const uint8_t* brow = xs + 32 + 512 * J.nch;
     uint32_t cr = 0;
 #pragma unroll 1
     for (int c = 0; c < J.nch; c++) {
@@ -348,7 +349,7 @@ __device__ __forceinline__ void emit_stash(const RowsJob& J, int j, int lane, co
 
 // Row j of the job: the five costs (pass 1), the winner, its residuals.
 template <int K, int DW>
-__device__ void filter_row(const WinCtx& w, const RowsJob& J, int j, int lane, uint8_t* xs)
+__device__ void filter_row(const WinCtx& w, const RowsJob& J, int j, int lane)
 {
     const uint8_t* xr = J.raw + (size_t)j * J.sp;
     const uint32_t K80 = 0x80808080u;
@@ -370,10 +371,6 @@ __device__ void filter_row(const WinCtx& w, const RowsJob& J, int j, int lane, u
         uint32_t x[4], b[4];
         win_raw<K>(w, cx, nv, x);
         win_above<K>(w, cb, am, nv, b);
-        if (xs) {
-            *reinterpret_cast<uint4*>(xs + 16 + 16 * u) = make_uint4(x[0], x[1], x[2], x[3]);
-            *reinterpret_cast<uint4*>(xs + 32 + 512 * J.nch + 16 * u) = make_uint4(b[0], b[1], b[2], b[3]);
-        }
         uint32_t xm1, xm2, bm1, bm2;
         left_of<DW>(x, lane, cx1, cx2, xm1, xm2);
         left_of<DW>(b, lane, cb1, cb2, bm1, bm2);
@@ -414,18 +411,6 @@ __device__ void filter_row(const WinCtx& w, const RowsJob& J, int j, int lane, u
     if (t2 < best) { best = t2; f = 2; }
     if (t3 < best) { best = t3; f = 3; }
     if (t4 < best) { f = 4; }
-    if (xs) {
-        __syncwarp();
-        switch (f) {
-            case 0: emit_stash<DW, 0>(J, j, lane, xs); break;
-            case 1: emit_stash<DW, 1>(J, j, lane, xs); break;
-            case 2: emit_stash<DW, 2>(J, j, lane, xs); break;
-            case 3: emit_stash<DW, 3>(J, j, lane, xs); break;
-            default: emit_stash<DW, 4>(J, j, lane, xs); break;
-        }
-        __syncwarp();     // the next row's pass 1 overwrites the stash
-        return;
-    }
     switch (f) {
         case 0: emit_row<K, DW, 0>(w, J, j, lane); break;
         case 1: emit_row<K, DW, 1>(w, J, j, lane); break;
@@ -435,18 +420,134 @@ __device__ void filter_row(const WinCtx& w, const RowsJob& J, int j, int lane, u
     }
 }
 
+// Chunks c0, c0 + step, ... of raw row `rowp` windowed into a stash slot's
+// data at dst (32 units a chunk, zeros past the row end), loads one chunk
+// ahead.
 template <int K>
-__device__ __forceinline__ void filter_rows_k(const WinCtx& w, const RowsJob& J, int r0, int r1, int warp, int nw,
-                                              int lane, int dw, uint8_t* xs)
+__device__ __forceinline__ void window_into(const WinCtx& w, const RowsJob& J, const uint8_t* rowp, int lane,
+                                            uint8_t* dst, int c0, int step)
 {
-    for (int j = r0 + warp; j < r1; j += nw) {
-        if (dw == 1) filter_row<K, 1>(w, J, j, lane, xs);
-        else         filter_row<K, 2>(w, J, j, lane, xs);
+    RawU nx = fetch_unit<K>(rowp, 32 * c0 + lane, J.rb - 16 * (32 * c0 + lane));
+#pragma unroll 1
+    for (int c = c0; c < J.nch; c += step) {
+        const int u = 32 * c + lane;
+        const int nv = J.rb - 16 * u;
+        const RawU cx = nx;
+        if (c + step < J.nch) nx = fetch_unit<K>(rowp, u + 32 * step, nv - 512 * step);
+        uint32_t x[4];
+        win_raw<K>(w, cx, nv, x);
+        *reinterpret_cast<uint4*>(dst + 16 * u) = make_uint4(x[0], x[1], x[2], x[3]);
     }
 }
 
-// Dynamic shared memory: the window table (lut_region bytes), then one
-// stash of `stash` bytes per warp (0: rows are windowed again in pass 2).
+// Rows [r0, r1) (at most kRowsWarps) through the CTA's stash: pass 0 windows
+// warp w's row r0 + w into slot 1 + w, and every warp a share of the chunks
+// of the row above r0 into slot 0 (the windowed raw row, the caller's prior
+// row, or zeros); after one CTA barrier pass 1 scores each row from its slot
+// and the slot before it, and pass 2 forms the winner's residuals from the
+// same two slots.  Every row is windowed once.  All warps of the CTA call
+// this.
+template <int K, int DW>
+__device__ void filter_item_stash(const WinCtx& w, const RowsJob& J, int r0, int r1, int warp, int lane,
+                                  uint8_t* stash)
+{
+    const int slot = rows_slot_bytes(J.nch);
+    const int j = r0 + warp;
+    const bool has = j < r1;
+    uint8_t* xs = stash + (1 + warp) * slot;
+    if (lane == 0) *reinterpret_cast<uint4*>(xs) = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0 && lane == 1) *reinterpret_cast<uint4*>(stash) = make_uint4(0u, 0u, 0u, 0u);
+    if (has) window_into<K>(w, J, J.raw + (size_t)j * J.sp, lane, xs + 16, 0, 1);
+    uint8_t* bs = stash + 16;
+    if (r0 > 0) {
+        if (warp < J.nch) window_into<K>(w, J, J.raw + (size_t)(r0 - 1) * J.sp, lane, bs, warp, kRowsWarps);
+    } else {
+#pragma unroll 1
+        for (int u = 32 * warp + lane; u < 32 * J.nch; u += 32 * kRowsWarps) {
+            const int nv = J.rb - 16 * u;
+            const RawU r = (J.prior && nv > 0) ? fetch_prior(J.prior, u, nv)
+                                               : RawU{make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+            *reinterpret_cast<uint4*>(bs + 16 * u) = r.a;
+        }
+    }
+    __syncthreads();
+    if (!has) return;
+    const uint8_t* xrow = xs + 16;
+    const uint8_t* brow = xs - slot + 16;
+    const uint32_t K80 = 0x80808080u;
+    uint32_t S0 = 0, S1 = 0, S2 = 0, S3 = 0, S4 = 0;
+#pragma unroll 1
+    for (int c = 0; c < J.nch; c++) {
+        const int u = 32 * c + lane;
+        const int nv = J.rb - 16 * u;
+        const uint4 xv = *reinterpret_cast<const uint4*>(xrow + 16 * u);
+        const uint4 bv = *reinterpret_cast<const uint4*>(brow + 16 * u);
+        const uint2 xm = *reinterpret_cast<const uint2*>(xrow + 16 * u - 8);
+        const uint2 bm = *reinterpret_cast<const uint2*>(brow + 16 * u - 8);
+        const uint32_t x[4] = {xv.x, xv.y, xv.z, xv.w}, b[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t a = left_word(x, xm.y, xm.x, DW, J.sh, q);
+            const uint32_t cq = left_word(b, bm.y, bm.x, DW, J.sh, q);
+            const uint32_t av = avg4_dev(a, b[q]);
+            const uint32_t pp = paeth_word(a, b[q], cq, widen_lo(a), widen_hi(a), widen_lo(b[q]), widen_hi(b[q]),
+                                           widen_lo(cq), widen_hi(cq));
+            uint32_t d1 = __vabsdiffu4(x[q], a), d2 = __vabsdiffu4(x[q], b[q]);
+            uint32_t d3 = __vabsdiffu4(x[q], av), d4 = __vabsdiffu4(x[q], pp);
+            if (nv < 16) {
+                // bytes past the row end: x = 0 and d = 0 add 128 - |0 - 128| = 0
+                const uint32_t m = valid_mask(nv, q);
+                d1 &= m;
+                d2 &= m;
+                d3 &= m;
+                d4 &= m;
+            }
+            S0 = sad4(x[q], K80, S0);
+            S1 = sad4(d1, K80, S1);
+            S2 = sad4(d2, K80, S2);
+            S3 = sad4(d3, K80, S3);
+            S4 = sad4(d4, K80, S4);
+        }
+    }
+    const uint32_t base = 2048u * (uint32_t)J.nch;
+    const uint32_t t0 = __reduce_add_sync(kFull, base - S0);
+    const uint32_t t1 = __reduce_add_sync(kFull, base - S1);
+    const uint32_t t2 = __reduce_add_sync(kFull, base - S2);
+    const uint32_t t3 = __reduce_add_sync(kFull, base - S3);
+    const uint32_t t4 = __reduce_add_sync(kFull, base - S4);
+    int f = 0;
+    uint32_t best = t0;
+    if (t1 < best) { best = t1; f = 1; }
+    if (t2 < best) { best = t2; f = 2; }
+    if (t3 < best) { best = t3; f = 3; }
+    if (t4 < best) { f = 4; }
+    switch (f) {
+        case 0: emit_stash<DW, 0>(J, j, lane, xrow, brow); break;
+        case 1: emit_stash<DW, 1>(J, j, lane, xrow, brow); break;
+        case 2: emit_stash<DW, 2>(J, j, lane, xrow, brow); break;
+        case 3: emit_stash<DW, 3>(J, j, lane, xrow, brow); break;
+        default: emit_stash<DW, 4>(J, j, lane, xrow, brow); break;
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void filter_rows_k(const WinCtx& w, const RowsJob& J, int r0, int r1, int warp, int nw,
+                                              int lane, int dw, uint8_t* stash)
+{
+    if (stash) {
+        if (dw == 1) filter_item_stash<K, 1>(w, J, r0, r1, warp, lane, stash);
+        else         filter_item_stash<K, 2>(w, J, r0, r1, warp, lane, stash);
+        return;
+    }
+    for (int j = r0 + warp; j < r1; j += nw) {
+        if (dw == 1) filter_row<K, 1>(w, J, j, lane);
+        else         filter_row<K, 2>(w, J, j, lane);
+    }
+}
+
+// Dynamic shared memory: the window table (lut_region bytes), then the CTA's
+// stash of `stash` bytes (0: no stash; rows are then windowed again in
+// pass 2).
 __global__ void __launch_bounds__(kRowsThreads, 3)
 k_filter_rows(DevImage* __restrict__ imgs, const BandItem* __restrict__ items, int nitems, int lut_region, int stash)
 {
@@ -502,13 +603,9 @@ k_filter_rows(DevImage* __restrict__ imgs, const BandItem* __restrict__ items, i
         const int dw = (d.bpp + 3) >> 2;
         J.sh = 8u * (uint32_t)(4 * dw - d.bpp);
         const int r0 = (int)bi.r0, r1 = (int)bi.r1;
-        uint8_t* xs = nullptr;
-        if (stash >= rows_stash_bytes(J.nch)) {
-            xs = lut + lut_region + warp * stash;
-            if (lane == 0) *reinterpret_cast<uint4*>(xs) = make_uint4(0u, 0u, 0u, 0u);
-            if (lane == 1) *reinterpret_cast<uint4*>(xs + 16 + 512 * J.nch) = make_uint4(0u, 0u, 0u, 0u);
-            __syncwarp();
-        }
+        // the stash path takes an item of at most one row per warp (the
+        // host's items); the condition is the same in every thread
+        uint8_t* xs = (stash >= rows_stash_bytes(J.nch) && r1 - r0 <= kRowsWarps) ? lut + lut_region : nullptr;
         switch (kind) {
             case K_LUT16Z: filter_rows_k<K_LUT16Z>(wc, J, r0, r1, warp, kRowsWarps, lane, dw, xs); break;
             case K_COPY: filter_rows_k<K_COPY>(wc, J, r0, r1, warp, kRowsWarps, lane, dw, xs); break;
@@ -553,16 +650,16 @@ int rows_filter_rows_per_item() { return kRowsWarps; }
 
 int rows_filter_lut_region(int lut_bytes) { return (std::min(lut_bytes, kRowsLutMax) + 15) & ~15; }
 
-// Per-warp stash for rows of rb filtered bytes, or 0 when the launch could
-// then not keep two CTAs on an SM (rows of more than about 6 KB): those rows
-// are windowed again in pass 2 instead.
+// A CTA's stash for rows of rb filtered bytes, or 0 when the launch could
+// then not keep three CTAs on an SM (rows of more than about 7 KB with an
+// 8 KB table): those rows are windowed again in pass 2 instead.
 int rows_filter_stash(int rb, int lut_bytes)
 {
     const int st = rows_stash_bytes((rb + 511) / 512);
-    return rows_filter_lut_region(lut_bytes) + kRowsWarps * st <= kRowsSmemMax ? st : 0;
+    return rows_filter_lut_region(lut_bytes) + st <= kRowsSmemMax ? st : 0;
 }
 
-int rows_filter_smem(int lut_bytes, int stash) { return rows_filter_lut_region(lut_bytes) + kRowsWarps * stash; }
+int rows_filter_smem(int lut_bytes, int stash) { return rows_filter_lut_region(lut_bytes) + stash; }
 
 int rows_filter_ctas_per_sm(int smem)
 {
