@@ -213,7 +213,7 @@ KERNELS = ["k_prepare_window", "k_window_filter", "k_stored_blocks", "k_lz77_blo
 
 def filter_kernel(img):
     """The filter kernel the engine runs for img (pixels 16-byte aligned):
-    k_filter_rows for rows of 4096 filtered bytes or more whose raw row is a
+    k_filter_rows for rows of 2048 filtered bytes or more whose raw row is a
     multiple of 16 bytes and whose window table fits 32 KB; else
     k_window_filter_reg for rows of up to 8 KB with a table of up to 16 KB;
     else k_window_filter."""
@@ -224,7 +224,7 @@ def filter_kernel(img):
         lut = ((1 << bs if bs < 16 else 65536) if img.bytes_per_sample == 2 else 256) * img.out_bytes_per_sample
     elif img.window_mode == WINDOW_BATCH8:
         lut = 1 << bs
-    if img.row_bytes >= 4096 and pitch % 16 == 0 and lut <= 32768:
+    if img.row_bytes >= 2048 and pitch % 16 == 0 and lut <= 32768:
         return "k_filter_rows"
     ok = img.row_bytes <= 8192 and pitch % 16 == 0 and lut <= 16384
     return "k_window_filter_reg" if ok else "k_window_filter"

@@ -1,4 +1,4 @@
-"""The warp-per-row window + filter kernel (rows of 4096 filtered bytes and
+"""The warp-per-row window + filter kernel (rows of 2048 filtered bytes and
 more), bit-exact against the oracle's restatement of the reference
 (windowing src/gpu_filter.cu:71-162 and src/batch_processor.cpp:100-266;
 filter src/gpu_filter.cu:183-309; prior-row carry src/gpu_filter.cu:391-434).
@@ -32,7 +32,7 @@ def filter_guarded(r2p, engine, img, raw, prior=None):
 
 
 def check_rows(O, r2p, engine, img, raw, prior=None):
-    assert img.row_bytes >= 4096
+    assert img.row_bytes >= 2048
     want, _ = expected_filtered(O, r2p, img, raw, prior)
     got = filter_guarded(r2p, engine, img, raw, prior)
     if not np.array_equal(got, want):
@@ -117,10 +117,12 @@ def test_rows_dicom16_8bit_samples(O, r2p, engine):
     check_rows(O, r2p, engine, r2p.Image.make(4128, 9, 1, 1, r2p.WINDOW_DICOM16, dp), raw)
 
 
-@pytest.mark.parametrize("w,wc,ww", [(4104, 40.0, 400.0), (4104, 60.0, 150.0), (5000, -600.0, 1500.0)])
+@pytest.mark.parametrize("w,wc,ww", [(4104, 40.0, 400.0), (4104, 60.0, 150.0), (5000, -600.0, 1500.0),
+                                     (2048, 40.0, 400.0), (3072, -100.0, 700.0), (2056, 60.0, 150.0)])
 def test_rows_batch8(O, r2p, engine, W, w, wc, ww):
-    # 16-bit samples to 8-bit rows: Q15 (WW 400, 1500) or the FP32 table
-    # (WW 150); 4104 leaves a half unit at each row's end
+    # 16-bit samples to 8-bit rows: Q15 (WW 400, 1500, 700) or the FP32 table
+    # (WW 150); 4104 and 2056 leave a half unit at each row's end; 2048 and
+    # 3072 are the CT batch's two largest slice widths
     h = 17
     raw = W.ct_phantom(11, w, h)
     img = W.image_ct8(w, h, wc, ww)
