@@ -421,22 +421,31 @@ __device__ void filter_row(const WinCtx& w, const RowsJob& J, int j, int lane)
 }
 
 // Chunks c0, c0 + step, ... of raw row `rowp` windowed into a stash slot's
-// data at dst (32 units a chunk, zeros past the row end), loads one chunk
-// ahead.
+// data at dst (32 units a chunk, zeros past the row end).  Windowing costs
+// few instructions per load, so four chunks' loads (two for 16-bit samples to
+// 8-bit rows) are issued before any of them is windowed.
 template <int K>
 __device__ __forceinline__ void window_into(const WinCtx& w, const RowsJob& J, const uint8_t* rowp, int lane,
                                             uint8_t* dst, int c0, int step)
 {
-    RawU nx = fetch_unit<K>(rowp, 32 * c0 + lane, J.rb - 16 * (32 * c0 + lane));
+    constexpr int G = (K == K_Q15 || K == K_LUT8) ? 2 : 4;    // 32 raw bytes a unit there
 #pragma unroll 1
-    for (int c = c0; c < J.nch; c += step) {
-        const int u = 32 * c + lane;
-        const int nv = J.rb - 16 * u;
-        const RawU cx = nx;
-        if (c + step < J.nch) nx = fetch_unit<K>(rowp, u + 32 * step, nv - 512 * step);
-        uint32_t x[4];
-        win_raw<K>(w, cx, nv, x);
-        *reinterpret_cast<uint4*>(dst + 16 * u) = make_uint4(x[0], x[1], x[2], x[3]);
+    for (int c = c0; c < J.nch; c += G * step) {
+        RawU r[G];
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            const int u = 32 * (c + k * step) + lane;
+            r[k] = fetch_unit<K>(rowp, u, c + k * step < J.nch ? J.rb - 16 * u : 0);
+        }
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            if (c + k * step < J.nch) {
+                const int u = 32 * (c + k * step) + lane;
+                uint32_t x[4];
+                win_raw<K>(w, r[k], J.rb - 16 * u, x);
+                *reinterpret_cast<uint4*>(dst + 16 * u) = make_uint4(x[0], x[1], x[2], x[3]);
+            }
+        }
     }
 }
 
