@@ -12,27 +12,29 @@
 //                     windowed prior row, or zeros)
 //
 // Design.  Rows are independent once the row above is known, so a warp
-// filters a whole row by itself and no warp ever waits for another:
-//   pass 1  the warp walks the row in chunks of 32 units (lane l holds the
-//           16 output bytes of unit 32 c + l), windows the unit of the row
-//           and of the row above straight from the raw pixels (16-byte
-//           read-only loads; the row above is mostly in L1/L2, its own warp
-//           having just read it), takes the bytes bpp to the left from the
-//           neighbouring lane (a shuffle) and sums the five filters' costs:
-//           two instructions per filter and word (vabsdiff4, then vabsdiff4
-//           with .add against 0x80808080: min(v, 256 - v) = 128 - |d - 128|
-//           with d = |x - p| per byte);
-//   choice  five warp reductions (redux) and the argmin, the same in every
-//           lane;
-//   pass 2  the row is walked again, windowed again and only the winner's
-//           residuals x - p are formed; each lane stores them as aligned
-//           4-byte words re-cut from its unit and the previous lane's last
-//           word, so a warp's stores cover whole words of the output and
-//           only the row's first and last few bytes are stored bytewise.
-// Windowing twice costs less than keeping the row anywhere: the table
-// lookups are two shared-memory loads per word, while a row buffer in shared
-// memory (2 rows per warp) would cap a 36 KB-row image at a few warps per SM.
-// The window table is built once per image by k_window_lut (a grid over the
+// filters a whole row by itself: lane l holds the 16 output bytes of unit
+// 32 c + l of each 512-byte chunk c, and a CTA of 8 warps takes an item of
+// 8 consecutive rows.
+//   pass 0  each row of the item is windowed once, straight from the raw
+//           pixels (16-byte read-only loads, several chunks in flight), into
+//           the CTA's stash in shared memory: slot 1 + w holds warp w's row,
+//           slot 0 the row above the item (windowed by all 8 warps, or the
+//           caller's prior row, or zeros); one CTA barrier follows;
+//   pass 1  each warp sums the five filters' costs of its row from its own
+//           slot and the slot before it (the row above): two instructions
+//           per filter and word (vabsdiff4, then vabsdiff4 with .add against
+//           0x80808080: min(v, 256 - v) = 128 - |d - 128| with d = |x - p|
+//           per byte); five warp reductions (redux) and the argmin, the same
+//           in every lane, pick the filter;
+//   pass 2  the winner's residuals x - p, from the same two slots, stored as
+//           aligned 4-byte words re-cut from the lane's unit and the previous
+//           lane's last word (only a row's first and last few bytes are
+//           stored bytewise).
+// With an 8 KB table a CTA of 6 KB rows holds 64 KB, so three fit an SM.
+// Rows too wide for that (C2's 36000-byte rows) skip the stash: pass 1
+// windows the row and the row above from the raw pixels (one chunk ahead,
+// the bytes to the left by a shuffle) and pass 2 windows them again.  The
+// window table is built once per image by k_window_lut (a grid over the
 // table's entries) and copied into each CTA's shared memory.
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
