@@ -7,12 +7,15 @@
 // call builds a plan on the host (per image: geometry, window request, row
 // bands for the filter kernel, DEFLATE blocks), uploads it in one copy, and
 // launches one kernel per stage over the whole work list:
-//   [k_prepare_window ->] k_window_filter_reg | k_window_filter
+//   [k_window_lut -> k_filter_rows] | k_window_filter_reg | [k_prepare_window ->] k_window_filter
 //   -> k_stored_blocks | k_lz77_blocks | k_rle_dyn_blocks -> k_finish
-// (k_finish gathers the compressed blocks into the output, joins the
-// per-block checksums and writes the PNG chunks;
-// k_prepare_window builds window tables in HBM for the shared-memory filter
-// kernel and the BMP export; the register-resident kernel builds its own.)
+// (every image goes to one filter kernel: rows of kRowsMinRowBytes and more
+// whose pixels a 16-byte load may read to k_filter_rows, after k_window_lut
+// has built their window tables; other 16-byte-aligned rows of up to 8 KB to
+// the register-group kernel, which builds its own table; the rest to the
+// shared-memory kernel, whose tables k_prepare_window builds in HBM, as it
+// does for the BMP export.  k_finish gathers the compressed blocks into the
+// output, joins the per-block checksums and writes the PNG chunks.)
 // Calls are ordered through the engine: each call waits (on the device, not
 // the host) for the previous call's last kernel before reusing the arena.
 #include <cuda_runtime.h>
@@ -275,9 +278,9 @@ void plan_work(r2p_engine* e, std::vector<ImgPlan>& plans, const CallBuffers& cb
                       Prepared& P)
 {
     const int n = (int)plans.size();
-    // images whose rows fit the register-resident kernel (and whose pixels a
-    // bulk copy may read: 16-byte aligned) go there, the rest to the
-    // shared-memory kernel
+    // each image to one filter kernel: wide rows to the warp-per-row kernel,
+    // rows that fit the register-group kernel (and whose pixels a bulk copy
+    // may read: 16-byte aligned) there, the rest to the shared-memory kernel
     std::vector<char> use_reg((size_t)n, 0);
     int max_w = 0, nreg = 0;
     for (int i = 0; i < n; i++) {

@@ -24,6 +24,7 @@ int filter_lut_region(int mode, int lut_entries, int lut_esize);
 int filter_ctas_per_sm(int smem);
 
 // k_filter_reg.cu: rows of up to 8 KB held in registers by groups of warps
+// (the engine sends it the rows narrower than the warp-per-row kernel's)
 int reg_filter_warps(int rb);
 bool reg_filter_eligible(int rb, int in_pitch, int lut_bytes);
 int reg_filter_cta_warps(int max_w);
