@@ -284,38 +284,53 @@ __device__ __forceinline__ void emit_row(const WinCtx& w, const RowsJob& J, int 
 __host__ __device__ inline int rows_slot_bytes(int nch) { return 16 + 512 * nch; }
 __host__ __device__ inline int rows_stash_bytes(int nch) { return (kRowsWarps + 1) * rows_slot_bytes(nch); }
 
-// Pass 2 for filter F from the stash: row j's windowed bytes at xrow, the
-// row above at brow (each with 16 zero bytes before it).
-template <int DW, int F>
-__device__ __forceinline__ void emit_stash(const RowsJob& J, int j, int lane, const uint8_t* xrow,
-                                           const uint8_t* brow)
+// 16 and 8 bytes from shared memory at 32-bit shared address a.
+__device__ __forceinline__ uint4 lds128(uint32_t a)
 {
-    uint8_t* R = J.filt + (size_t)j * (size_t)(J.rb + 1);
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ uint2 lds64(uint32_t a)
+{
+    uint2 v;
+    asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+    return v;
+}
+
+// Pass 2 for filter F from the stash: row j's windowed bytes at shared
+// address xa, the row above at ba (each with 16 zero bytes before it).  One
+// copy per (DW, F), called once per row: it does not depend on the window.
+template <int DW, int F>
+__device__ __noinline__ void emit_stash(uint8_t* filt, uint8_t* last_row, int rb, int height, int nch, uint32_t sh,
+                                        int j, int lane, uint32_t xa, uint32_t ba)
+{
+    uint8_t* R = filt + (size_t)j * (size_t)(rb + 1);
     if (lane == 0) R[0] = (uint8_t)F;
-    const bool keep_last = J.last_row != nullptr && j == J.height - 1;
+    const bool keep_last = last_row != nullptr && j == height - 1;
     uint32_t cr = 0;
 #pragma unroll 1
-    for (int c = 0; c < J.nch; c++) {
+    for (int c = 0; c < nch; c++) {
         const int u = 32 * c + lane;
-        const int nv = J.rb - 16 * u;
-        const uint4 xv = *reinterpret_cast<const uint4*>(xrow + 16 * u);
+        const int nv = rb - 16 * u;
+        const uint4 xv = lds128(xa + 16 * u);
         const uint32_t x[4] = {xv.x, xv.y, xv.z, xv.w};
         uint32_t b[4] = {0u, 0u, 0u, 0u};
         uint32_t xm1 = 0, xm2 = 0, bm1 = 0, bm2 = 0;
         if (F == 1 || F >= 3) {
-            const uint2 m = *reinterpret_cast<const uint2*>(xrow + 16 * u - 8);
+            const uint2 m = lds64(xa + 16 * u - 8);
             xm2 = m.x;
             xm1 = m.y;
         }
         if (F >= 2) {
-            const uint4 bv = *reinterpret_cast<const uint4*>(brow + 16 * u);
+            const uint4 bv = lds128(ba + 16 * u);
             b[0] = bv.x;
             b[1] = bv.y;
             b[2] = bv.z;
             b[3] = bv.w;
         }
         if (F == 4) {
-            const uint2 m = *reinterpret_cast<const uint2*>(brow + 16 * u - 8);
+            const uint2 m = lds64(ba + 16 * u - 8);
             bm2 = m.x;
             bm1 = m.y;
         }
@@ -325,14 +340,14 @@ __device__ __forceinline__ void emit_stash(const RowsJob& J, int j, int lane, co
             if (F == 0) {
                 r[q] = x[q];
             } else if (F == 1) {
-                r[q] = __vsub4(x[q], left_word(x, xm1, xm2, DW, J.sh, q));
+                r[q] = __vsub4(x[q], left_word(x, xm1, xm2, DW, sh, q));
             } else if (F == 2) {
                 r[q] = __vsub4(x[q], b[q]);
             } else if (F == 3) {
-                r[q] = __vsub4(x[q], avg4_dev(left_word(x, xm1, xm2, DW, J.sh, q), b[q]));
+                r[q] = __vsub4(x[q], avg4_dev(left_word(x, xm1, xm2, DW, sh, q), b[q]));
             } else {
-                const uint32_t a = left_word(x, xm1, xm2, DW, J.sh, q);
-                const uint32_t cq = left_word(b, bm1, bm2, DW, J.sh, q);
+                const uint32_t a = left_word(x, xm1, xm2, DW, sh, q);
+                const uint32_t cq = left_word(b, bm1, bm2, DW, sh, q);
                 r[q] = __vsub4(x[q], paeth_word(a, b[q], cq, widen_lo(a), widen_hi(a), widen_lo(b[q]),
                                                 widen_hi(b[q]), widen_lo(cq), widen_hi(cq)));
             }
@@ -341,9 +356,9 @@ __device__ __forceinline__ void emit_stash(const RowsJob& J, int j, int lane, co
         if (lane == 0) rp = cr;
         cr = __shfl_sync(kFull, r[3], 31);
         if (nv > 0) {
-            store_unit(R, J.rb, u, r, rp);
+            store_unit(R, rb, u, r, rp);
             if (keep_last) {
-                for (int k = 0; k < 16 && k < nv; k++) J.last_row[16 * u + k] = (uint8_t)(x[k >> 2] >> (8 * (k & 3)));
+                for (int k = 0; k < 16 && k < nv; k++) last_row[16 * u + k] = (uint8_t)(x[k >> 2] >> (8 * (k & 3)));
             }
         }
     }
@@ -532,12 +547,13 @@ __device__ void filter_item_stash(const WinCtx& w, const RowsJob& J, int r0, int
     if (t2 < best) { best = t2; f = 2; }
     if (t3 < best) { best = t3; f = 3; }
     if (t4 < best) { f = 4; }
+    const uint32_t xa = (uint32_t)__cvta_generic_to_shared(xrow), ba = (uint32_t)__cvta_generic_to_shared(brow);
     switch (f) {
-        case 0: emit_stash<DW, 0>(J, j, lane, xrow, brow); break;
-        case 1: emit_stash<DW, 1>(J, j, lane, xrow, brow); break;
-        case 2: emit_stash<DW, 2>(J, j, lane, xrow, brow); break;
-        case 3: emit_stash<DW, 3>(J, j, lane, xrow, brow); break;
-        default: emit_stash<DW, 4>(J, j, lane, xrow, brow); break;
+        case 0: emit_stash<DW, 0>(J.filt, J.last_row, J.rb, J.height, J.nch, J.sh, j, lane, xa, ba); break;
+        case 1: emit_stash<DW, 1>(J.filt, J.last_row, J.rb, J.height, J.nch, J.sh, j, lane, xa, ba); break;
+        case 2: emit_stash<DW, 2>(J.filt, J.last_row, J.rb, J.height, J.nch, J.sh, j, lane, xa, ba); break;
+        case 3: emit_stash<DW, 3>(J.filt, J.last_row, J.rb, J.height, J.nch, J.sh, j, lane, xa, ba); break;
+        default: emit_stash<DW, 4>(J.filt, J.last_row, J.rb, J.height, J.nch, J.sh, j, lane, xa, ba); break;
     }
 }
 
