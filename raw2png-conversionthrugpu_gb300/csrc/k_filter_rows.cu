@@ -53,7 +53,7 @@ constexpr int kRowsWarps = 8;                  // warps per CTA: rows filtered s
 constexpr int kRowsThreads = 32 * kRowsWarps;
 constexpr int kRowsLutMax = 32768;             // table bytes a CTA keeps in shared memory
 constexpr int kRowsSmemMax = 74 * 1024;        // dynamic shared memory of a CTA: three fit an SM
-constexpr int kLutEntriesPerCta = 1024;        // k_window_lut: four entries per thread
+constexpr int kLutEntriesPerCta = 1024;        // k_window_lut: table bytes per CTA of 256 threads
 
 // Everything a warp needs about its image, in registers.
 struct RowsJob {
@@ -66,8 +66,9 @@ struct RowsJob {
 };
 
 // Raw bytes of one unit: 16 (a = all; same depth in and out) or 32 (a, b;
-// 16-bit samples to an 8-bit row).  Loads are issued one chunk ahead of the
-// arithmetic that uses them, so a warp's row walk keeps a load in flight.
+// 16-bit samples to an 8-bit row).  The row walks issue these loads ahead of
+// the arithmetic that uses them (one chunk ahead in the wide-row passes,
+// four chunks at a time in pass 0 of the stash path).
 struct RawU {
     uint4 a, b;
 };
