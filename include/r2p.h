@@ -141,9 +141,10 @@ void   r2p_batch_destroy(r2p_batch* b);
  * takes everything larger), the DEFLATE block size used for a level-1 image
  * whose block_size is 0 (levels 0 and 2-9 keep 65520-byte blocks: fewer
  * stored headers, and per-block Huffman codes that pay for their header),
- * the filter's rows per work item (0 = about 64 KB of
- * filtered output per item; a work list with fewer items than resident CTA
- * slots is split evenly over them instead) and
+ * the filter's rows per work item of the shared-memory filter kernel (0 =
+ * about 64 KB of filtered output per item; a work list with fewer items than
+ * resident CTA slots is split evenly over them instead; the row-per-warp and
+ * register-group kernels size their items from the row width) and
  * the LZ77 hash-table bits per image (9 or 10: 2^9 or 2^10 entries per
  * warp).  Set from the
  * autotuner's table; n = 0 restores the built-in one (the autotuner's GB300
@@ -349,7 +350,7 @@ int  r2p_stream_wait_event(void* stream, void* ev);   /* later work on stream wa
  * them, returns per-stage device milliseconds summed over the calls since the
  * last query (and how many launches each sum covers), and resets. */
 #define R2P_STAGE_PREPARE  0   /* k_prepare_window: window tables (shared-memory filter, BMP) */
-#define R2P_STAGE_FILTER   1   /* k_window_filter / k_window_filter_reg: window + adaptive filter */
+#define R2P_STAGE_FILTER   1   /* k_window_lut + k_filter_rows / k_window_filter_reg / k_window_filter: window + adaptive filter */
 #define R2P_STAGE_STORED   2   /* k_stored_blocks: level-0 DEFLATE */
 #define R2P_STAGE_LZ77     3   /* k_lz77_blocks (level 1) and k_rle_dyn_blocks (2..9) */
 #define R2P_STAGE_FINALIZE 4   /* k_finish: block gather, checksum combine, PNG chunks */
